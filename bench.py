@@ -1,0 +1,292 @@
+"""Benchmark of the GB300 lattice Boltzmann time step.
+
+Workload (one GPU): a batch of seeded 1024x1024 pore images of the multi-block
+configuration (disk radii U[6,40], porosity U[0.5,0.7], 3-level quadtree,
+Kn U[0.01,1]); the batch is sized so that its state is larger than L2.
+A bench step is one coarse time step of every image of the batch.
+
+  value     MLUPS over the batch, device-timed with CUDA events around K steps
+            replayed from CUDA graphs (state resident in HBM)
+  e2e       MLUPS through the public C ABI with host buffers: per image the
+            equilibrium state is uploaded (mgpu_set_equilibrium), K steps run
+            with the reference's per-step residual and break test (mgpu_run),
+            and the per-cell fields are read back (mgpu_download_cells)
+  roofline  the finest-level step kernel: 72 B per lattice update (9 FP32
+            populations read + 9 written) over its CUDA-event launch time
+  cpu_baseline  the FP64 CPU oracle (a restatement of the reference's step)
+            on the host cores, on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone, as the reference arm.
+Multi-GPU (torchrun): every rank runs its own batch (weak scaling, no
+collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_LU = 72.0
+WORKLOAD = "config2: 1024x1024 seeded disk images (r U[6,40], porosity U[0.5,0.7]), 3-level quadtree, Kn U[0.01,1]"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def start(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([v.strip() for v in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+
+        self._th = threading.Thread(target=run, daemon=True)
+        self._th.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and "Active" in r[2 + i]
+                          and "Not" not in r[2 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_images(count, offset):
+    from mantiis_gb300 import workloads
+
+    return [workloads.config2(offset + i) for i in range(count)]
+
+
+def params_for(img):
+    from mantiis_gb300 import default_params
+
+    return default_params(multiblock=1, max_allowed_level=3, dx=img["dx"])
+
+
+def cpu_oracle_rate(img, seconds, threads):
+    """MLUPS of the FP64 oracle on one image, steps sized to ~`seconds`."""
+    from mantiis_gb300 import HostGrid, Solver  # noqa: F401
+    from oracle.pyoracle import for_grid
+
+    p = params_for(img)
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
+    lu = float(np.sum([(1 << (g.max_level - l)) for l, b in zip(g.cells["level"], g.cells["is_buffer"]) if not b]))
+    o = for_grid(g, sim="transport", dx=img["dx"], threads=threads)
+    t0 = time.perf_counter()
+    o.run(1)
+    t1 = time.perf_counter()
+    per = max(t1 - t0, 1e-6)
+    steps = max(2, int(seconds / per))
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return lu * steps / dt / 1e6, steps, dt, lu
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    img = make_images(1, 0)[0]
+    threads = os.cpu_count() or 1
+    samples = []
+    for _ in range(args.warmup):
+        cpu_oracle_rate(img, 2.0, threads)
+    for _ in range(args.steps):
+        samples.append(cpu_oracle_rate(img, args.ref_seconds, threads))
+    rate = float(np.median([s[0] for s in samples]))
+    steps = samples[-1][1]
+    line = {
+        "impl": "reference", "metric": "MLUPS", "value": rate, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "images": 1, "n": 1024, "levels": 3},
+        "cpu_baseline": {"value": rate, "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"1 image, {steps} coarse steps per measurement, FP64 oracle restatement "
+                                   f"of the reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads"},
+        "e2e": {"value": rate, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--images", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from mantiis_gb300 import Solver
+
+    imgs = make_images(args.images, rank * args.images)
+    stream = torch.cuda.current_stream()
+    solvers = []
+    for img in imgs:
+        s = Solver(img["pore"], img["kn"], img["locpore"], params_for(img))
+        s.set_stream(stream.cuda_stream)
+        solvers.append(s)
+    lu_step = float(sum(s.info["lu_per_step"] for s in solvers))
+    state_mb = sum(s.info["device_bytes"] for s in solvers) / 1e6
+
+    # warm-up (also captures each context's CUDA graph)
+    warm = args.warmup + (args.warmup % 2)
+    for s in solvers:
+        s.advance_graph(warm)
+    torch.cuda.synchronize()
+    K = args.steps + (args.steps % 2)
+    l0 = sum(s.launches for s in solvers)
+    clk = ClockSampler(local)
+    clk.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in solvers:
+        s.advance_graph(K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    launches = sum(s.launches for s in solvers) - l0
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = lu_step * world * K / (ms / 1e3) / 1e6
+
+    # roofline: finest-level step kernel of image 0 on a separate context
+    prof = Solver(imgs[0]["pore"], imgs[0]["kn"], imgs[0]["locpore"], params_for(imgs[0]))
+    prof.set_stream(stream.cuda_stream)
+    prof.advance(2)
+    lvl1 = prof.level_info(1)
+    reps = 200
+    prof.step_level(1, 10)
+    torch.cuda.synchronize()
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    prof.step_level(1, reps)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    k_ms = r0.elapsed_time(r1) / reps
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_LU * lvl1["active"] / (k_ms / 1e3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("k_step_level1_bytes_per_launch")
+        except Exception:
+            traffic = None
+    prof.close()
+
+    # end to end through the public API with host buffers
+    Ke = args.e2e_steps
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for s, img in zip(solvers, imgs):
+        n = s.n_cells
+        rho = np.full(n, s.info["rho_in"])
+        z = np.zeros(n)
+        s.set_equilibrium(rho, z, z)
+        h2d += 3 * n * 8
+        s.run(Ke)
+        c = s.cells()
+        d2h += 3 * n * 8 + Ke * 4 * 8
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = lu_step * Ke / e2e_s / 1e6
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, steps, dt, lu = cpu_oracle_rate(imgs[0], args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"image 0 of the batch, {steps} coarse steps ({dt:.1f} s), FP64 oracle restatement of the "
+                         f"reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": warm,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "images_per_gpu": len(imgs), "n": 1024, "levels": 3,
+                       "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
+                       "l2": "inputs larger than L2 (state of the batch > 129 MB)", "graph": "CUDA graph of 2 coarse steps per image"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_step level 1", "units_per_launch": lvl1["active"],
+                         "bytes_per_unit": BYTES_PER_LU, "ms_per_launch": k_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,
+                    "steps": Ke, "seconds": e2e_s},
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line))
+    for s in solvers:
+        s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -27,4 +27,12 @@ constexpr double W[Q] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
 // Shan-Chen interaction weights (include/globalParameters.hpp:122)
 constexpr double WF[Q] = {0.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0,
                           1.0 / 12.0, 1.0 / 12.0, 1.0 / 12.0, 1.0 / 12.0};
+
+// the same numbers as functions, usable in device code (folded to constants
+// when q is a compile-time index)
+MGPU_HD constexpr int cx(int q) { return (q == 1 || q == 5 || q == 8) ? 1 : ((q == 3 || q == 6 || q == 7) ? -1 : 0); }
+MGPU_HD constexpr int cy(int q) { return (q == 2 || q == 5 || q == 6) ? 1 : ((q == 4 || q == 7 || q == 8) ? -1 : 0); }
+MGPU_HD constexpr int opp(int q) { return q == 0 ? 0 : (q < 5 ? (q + 1) % 4 + 1 : (q - 3) % 4 + 5); }
+MGPU_HD constexpr double w(int q) { return q == 0 ? 4.0 / 9.0 : (q < 5 ? 1.0 / 9.0 : 1.0 / 36.0); }
+MGPU_HD constexpr double wf(int q) { return q == 0 ? 0.0 : (q < 5 ? 1.0 / 3.0 : 1.0 / 12.0); }
 } // namespace d2q9

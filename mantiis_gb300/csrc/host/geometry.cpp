@@ -10,6 +10,8 @@
 #include <random>
 #include <stdexcept>
 
+#include "../boundary_tables.h"
+
 namespace mantiis
 {
 namespace
@@ -286,6 +288,40 @@ std::vector<int> shrink_binary(const std::vector<int> &img, int n, int factor)
     return out;
 }
 
+int64_t fill_untabulated_pixels(std::vector<int> &img, int n)
+{
+    static const int dx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1}, dy[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    static const int order[9] = {7, 3, 6, 4, 0, 2, 8, 1, 5};
+    std::vector<uint8_t> ok(512, 0);
+    ok[511] = 1;
+    for (int t = 0; t < MANTIIS_N_BND_TYPES; t++) ok[MANTIIS_BND_CODES[t]] = 1;
+    int64_t filled = 0;
+    bool changed = true;
+    while (changed)
+    {
+        changed = false;
+        for (int y = 0; y < n; y++)
+            for (int x = 0; x < n; x++)
+            {
+                if (!img[(size_t)y * n + x]) continue;
+                int code = 0;
+                for (int k = 0; k < 9; k++)
+                {
+                    int q = order[k];
+                    int xx = (x + dx[q] + n) % n, yy = (y + dy[q] + n) % n;
+                    code = (code << 1) | (img[(size_t)yy * n + xx] ? 1 : 0);
+                }
+                if (!ok[code])
+                {
+                    img[(size_t)y * n + x] = 0;
+                    filled++;
+                    changed = true;
+                }
+            }
+    }
+    return filled;
+}
+
 std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed)
 {
     std::mt19937_64 rng(seed);
@@ -316,6 +352,7 @@ std::vector<int> generate_disk_image(int n, double rmin, double rmax, double por
                 }
             }
     }
+    fill_untabulated_pixels(img, n);
     return img;
 }
 } // namespace mantiis

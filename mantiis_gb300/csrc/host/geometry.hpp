@@ -57,7 +57,14 @@ void local_pore_properties(const std::vector<int> &domain, int n, double dx, dou
 std::vector<int> shrink_binary(const std::vector<int> &img, int n, int factor);
 
 // Seeded disk packing: solid disks of radius uniform in [rmin, rmax] at
-// uniform centres are stamped into an all-void n x n image until the
-// porosity is at most `porosity`; rows 0 and n-1 are then made solid.
+// uniform centres are stamped into an all-void n x n image (rows 0 and n-1
+// solid) until the porosity is at most `porosity`.  Void pixels whose
+// 9-neighbour wall pattern is not one of the 52 tabulated boundary types are
+// then filled (the reference rejects such images, include/grid.hpp:1146-1150).
 std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed);
+
+// Fills void pixels whose neighbour pattern (periodic in x and y, as the
+// grid's neighbour table) is not tabulated, until none is left; returns the
+// number of pixels filled.
+int64_t fill_untabulated_pixels(std::vector<int> &img, int n);
 } // namespace mantiis

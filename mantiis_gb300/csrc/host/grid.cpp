@@ -113,6 +113,7 @@ void Builder::build_cells()
         decompose(0, 0, n, min_dist);
         value = leafimg;
     }
+    g.reconstructed = value;
 
     // include/grid.hpp:427-558: cells in raster order of first occurrence
     auto side_of = [&](int64_t v) -> int {

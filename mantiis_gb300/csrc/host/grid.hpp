@@ -49,6 +49,7 @@ struct Grid
     std::vector<double> kn, locpore, tau;
 
     std::vector<int64_t> solid_pixels; // sorted raster ids of solid pixels
+    std::vector<int64_t> reconstructed; // quadtree image: +leaf number (void), -leaf number (solid)
 
     // interface tables (rows of 5 ids; key = buffer type)
     std::vector<std::array<int64_t, 5>> parent_child;

@@ -1,0 +1,354 @@
+// Kernels of the lattice Boltzmann step (sm_103a): the fused AA-pattern
+// collide-and-stream, the output/residual pass, the coarse/fine interface
+// exchange and the equilibrium initialisation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace mantiis
+{
+namespace dev
+{
+constexpr int kMaxLevels = 4;
+
+struct AllLevels
+{
+    LevelView lv[kMaxLevels];
+    int parity[kMaxLevels]; // parity of the next step of each level
+    int direct[kMaxLevels]; // level holds f itself (no step since initialisation)
+};
+
+// Sum of two doubles over the block, then one atomic per block.
+__device__ __forceinline__ void block_add2(double a, double b, double *dst)
+{
+    __shared__ double sa[32], sb[32];
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+    {
+        sa[wid] = a;
+        sb[wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0)
+    {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sa[lane] : 0.0;
+        b = lane < nw ? sb[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0)
+        {
+            if (a != 0.0) atomicAdd(dst, a);
+            if (b != 0.0) atomicAdd(dst + 1, b);
+        }
+    }
+    __syncthreads();
+}
+
+// Loads the populations of a cell of level view L for a step (or a read) at
+// parity P.  Returns |tau_s| and, for special cells, a copy of the record.
+template <int P>
+__device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, int x, int y, int direct, int first_sub,
+                                           float df[9], bool &special, SpecialRec &rec)
+{
+    const int64_t s = site_of(L, x, y);
+    float tau = L.tau[s];
+    special = tau < 0.0f;
+    if (!special)
+    {
+        if (direct) load_raw<0>(L, x, y, df);
+        else load_raw<P>(L, x, y, df);
+        return tau;
+    }
+    rec = C.specials[L.spec[s]];
+    const uint32_t flags = rec.m1 >> 17;
+    if ((flags & SF_BUFFER) && (first_sub || direct))
+    {
+#pragma unroll
+        for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + rec.buf];
+    }
+    else if (direct)
+        load_raw<0>(L, x, y, df);
+    else
+        load_special<P>(L, C, rec, x, y, df);
+    return -tau;
+}
+
+// One lattice update of every active site of one level (transport step body:
+// equilibrium, regularized MRT / MRT / BGK collision, streaming, walls,
+// x-periodicity; include/coreLB.hpp:420-430, 646-792, 834-977, 1018-1054).
+// One thread per site, 32x8 sites per block, blocks over the active tiles.
+template <int P> __global__ void __launch_bounds__(256) k_step(LevelView L, Common C, StepOpt o)
+{
+    const int tile = L.tiles[blockIdx.x];
+    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
+    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    double r_diff = 0.0, r_norm = 0.0;
+    if (x < L.W && y < L.H && L.tau[site_of(L, x, y)] != 0.0f)
+    {
+        const int64_t s = site_of(L, x, y);
+        float df[9];
+        bool special;
+        SpecialRec rec;
+        const float tau_s = load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
+        float drho, rho, ux, uy;
+        macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
+        if (o.diff | o.store_u)
+        {
+            const float un = sqrtf(ux * ux + uy * uy);
+            if (o.diff)
+            {
+                r_diff = (double)fabsf(un - L.unorm[s]);
+                r_norm = (double)un;
+            }
+            if (o.store_u) L.unorm[s] = un;
+        }
+        if (o.snap_store)
+        {
+            L.snap[s] = drho;
+            L.snap[L.plane + s] = ux;
+            L.snap[2 * L.plane + s] = uy;
+        }
+        float edrho = drho, erho = rho, eux = ux, euy = uy;
+        if (o.snap_use)
+        {
+            edrho = L.snap[s];
+            erho = C.rho0 + edrho;
+            eux = L.snap[L.plane + s];
+            euy = L.snap[2 * L.plane + s];
+        }
+        float feq[9], fs[9];
+        equilibrium(edrho, erho, eux, euy, feq);
+        if (C.collision == COLL_RMRT) collide_rmrt(df, feq, tau_s, fs);
+        else if (C.collision == COLL_MRT) collide_mrt(df, feq, tau_s, L.tau2 ? L.tau2[s] : 1.0f, fs);
+        else
+        {
+            const float inv_tau = 1.0f; // 1 / tau_SRT, tau_SRT = 1 (include/globalParameters.hpp:140)
+#pragma unroll
+            for (int q = 0; q < 9; q++) fs[q] = df[q] - inv_tau * (df[q] - feq[q]);
+        }
+        if (special)
+        {
+            const uint32_t wall = (rec.m0 >> 18) & 0x1FFu, quirk = rec.m1 & 0x1FFu;
+            if (wall && C.wall == WALL_MDBB)
+            {
+                // include/coreLB.hpp:936-967: reflected value
+                //   r f*_q + (1 - r) (sum_{c.n<0} f / sum_{c.n>0} f_eq) f_eq,opp(q)
+                // in deviation form; both sums share the weight total A.
+                const uint32_t bnd = (rec.m1 >> 9) & 0xFFu;
+                const uint32_t pos = bnd == 0xFFu ? 0u : c_npos[bnd], neg = bnd == 0xFFu ? 0u : c_nneg[bnd];
+                float a = 0.f, ap = 0.f, A = 0.f;
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                {
+                    if ((neg >> q) & 1u) a += df[q];
+                    if ((pos >> q) & 1u)
+                    {
+                        ap += feq[q];
+                        A += wq(q) * C.rho0;
+                    }
+                }
+                const float g = (A + ap) != 0.f ? (a - ap) / (A + ap) : 0.f;
+                const float r = rec.r;
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                    if ((wall >> q) & 1u)
+                    {
+                        const int po = d2q9::opp(q);
+                        fs[q] = r * fs[q] + (1.0f - r) * (feq[po] + (wq(po) * C.rho0 + feq[po]) * g);
+                    }
+            }
+            if (quirk)
+            {
+                float *side_now = C.side + (size_t)P * C.n_quirk;
+                int qi = 0;
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                    if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
+            }
+        }
+        store_post<P>(L, x, y, fs);
+    }
+    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+}
+
+// Reads the current state of every reference cell (no update): FP64 density,
+// velocity and populations in reference cell order, plus the residual terms
+// against the stored |u| and the pixel-area sums of u_x and rho.
+__global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int32_t *cell_level, const int32_t *cell_site,
+                                               int64_t n, double *rho_out, double *ux_out, double *uy_out, double *f_out,
+                                               int diff, int store_u, int red_slot)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double r_diff = 0.0, r_norm = 0.0, r_ux = 0.0, r_rho = 0.0;
+    if (c < n)
+    {
+        const int l = cell_level[c] - 1;
+        const LevelView &L = A.lv[l];
+        const int s = cell_site[c];
+        const int x = s % L.pitch, y = s / L.pitch;
+        float df[9];
+        bool special;
+        SpecialRec rec;
+        // after a coarse step every interface buffer holds its interpolated values
+        if (A.parity[l] == 0) load_cell<0>(L, C, x, y, A.direct[l], 1, df, special, rec);
+        else load_cell<1>(L, C, x, y, A.direct[l], 1, df, special, rec);
+        float drho, rho, ux, uy;
+        macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
+        if (diff | store_u)
+        {
+            const float un = sqrtf(ux * ux + uy * uy);
+            if (diff)
+            {
+                r_diff = (double)fabsf(un - L.unorm[s]);
+                r_norm = (double)un;
+            }
+            if (store_u) L.unorm[s] = un;
+        }
+        // FP64 outputs from the FP32 deviations
+        double ddr = 0, jx = 0, jy = 0;
+        for (int q = 0; q < 9; q++)
+        {
+            ddr += (double)df[q];
+            jx += (double)d2q9::cx(q) * (double)df[q];
+            jy += (double)d2q9::cy(q) * (double)df[q];
+        }
+        const double r = (double)C.rho0 + ddr;
+        const double vx = (jx + (double)L.fshift) / r, vy = jy / r;
+        if (rho_out) rho_out[c] = r;
+        if (ux_out) ux_out[c] = vx;
+        if (uy_out) uy_out[c] = vy;
+        if (f_out)
+            for (int q = 0; q < 9; q++) f_out[c * 9 + q] = d2q9::w(q) * (double)C.rho0 + (double)df[q];
+        const bool buffer = special && ((rec.m1 >> 17) & SF_BUFFER);
+        if (!buffer)
+        {
+            const double area = (double)(1 << (2 * l));
+            r_ux = vx * area;
+            r_rho = r * area;
+        }
+    }
+    if (red_slot >= 0)
+    {
+        block_add2(r_diff, r_norm, C.red + red_slot);
+        block_add2(r_ux, r_rho, C.red + red_slot + 2);
+    }
+}
+
+// Coarse buffer cells <- rescaled mean of their 4 children
+// (include/coreLB.hpp:1104-1135): f_c = f_eq,c + 2 tau_c / mean(tau_f) (mean(f_f) - f_eq,c).
+template <int PF>
+__global__ void __launch_bounds__(128) k_coarse(LevelView Lf, LevelView Lc, Common C, const CoarseRowDev *rows, int nrows)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const CoarseRowDev row = rows[r];
+    float mean[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 4; k++)
+    {
+        if (row.child[k] < 0) continue;
+        float df[9];
+        if (row.child_buf[k] >= 0)
+        {
+#pragma unroll
+            for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + row.child_buf[k]];
+        }
+        else
+        {
+            bool special;
+            SpecialRec rec;
+            load_cell<PF>(Lf, C, row.child[k] % Lf.pitch, row.child[k] / Lf.pitch, 0, 0, df, special, rec);
+        }
+#pragma unroll
+        for (int q = 0; q < 9; q++) mean[q] += df[q];
+    }
+    const float drho = Lc.snap[row.site], ux = Lc.snap[Lc.plane + row.site], uy = Lc.snap[2 * Lc.plane + row.site];
+    float feq[9];
+    equilibrium(drho, C.rho0 + drho, ux, uy, feq);
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+        C.ibuf[(size_t)q * C.n_buf + row.buf] = feq[q] + row.ratio * (mean[q] * row.inv_nchild - feq[q]);
+}
+
+// Fine buffer cells <- bicubic spline of the parent neighbourhood
+// (include/coreLB.hpp:1137-1230); the spline is linear in the node values, so
+// each child holds 6 precomputed weights.  f = f_eq + tau_f / (2 tau_c) (f_spline - f_eq).
+template <int PC>
+__global__ void __launch_bounds__(128) k_fine(LevelView Lf, LevelView Lc, Common C, const FineRowDev *rows, int nrows)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const FineRowDev &row = rows[r];
+    float z[6][9];
+    for (int k = 0; k < 6; k++)
+    {
+        if (row.node_buf[k] >= 0)
+        {
+#pragma unroll
+            for (int q = 0; q < 9; q++) z[k][q] = C.ibuf[(size_t)q * C.n_buf + row.node_buf[k]];
+        }
+        else
+        {
+            bool special;
+            SpecialRec rec;
+            load_cell<PC>(Lc, C, row.node_site[k] % Lc.pitch, row.node_site[k] / Lc.pitch, 0, 0, z[k], special, rec);
+        }
+    }
+    for (int c = 0; c < 4; c++)
+    {
+        const int s = row.child_site[c];
+        const float drho = Lf.snap[s], ux = Lf.snap[Lf.plane + s], uy = Lf.snap[2 * Lf.plane + s];
+        float feq[9];
+        equilibrium(drho, C.rho0 + drho, ux, uy, feq);
+        const float rat = row.ratio[c];
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+        {
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < 6; k++) v += row.weight[c][k] * z[k][q];
+            C.ibuf[(size_t)q * C.n_buf + row.child_buf[c]] = feq[q] + rat * (v - feq[q]);
+        }
+    }
+}
+
+// f = f_eq(rho, u) per reference cell, written into its own slots (state then
+// reads "direct") and, for interface buffers, into the interpolation buffer.
+__global__ void k_set_equilibrium(AllLevels A, Common C, const int32_t *cell_level, const int32_t *cell_site, int64_t n,
+                                  const double *rho, const double *ux, const double *uy)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int l = cell_level[c] - 1;
+    const LevelView &L = A.lv[l];
+    const int s = cell_site[c];
+    const double r = rho[c], vx = ux[c], vy = uy[c];
+    const double usq = vx * vx + vy * vy;
+    float df[9];
+    for (int q = 0; q < 9; q++)
+    {
+        const double cu = d2q9::cx(q) * vx + d2q9::cy(q) * vy;
+        // deviation from w rho0, formed in FP64 before rounding
+        const double feq = d2q9::w(q) * r * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+        df[q] = (float)(feq - d2q9::w(q) * (double)C.rho0);
+        L.f[(size_t)q * L.plane + s] = df[q];
+    }
+    const float tau = L.tau[s];
+    if (tau < 0.0f)
+    {
+        const SpecialRec rec = C.specials[L.spec[s]];
+        if ((rec.m1 >> 17) & SF_BUFFER)
+            for (int q = 0; q < 9; q++) C.ibuf[(size_t)q * C.n_buf + rec.buf] = df[q];
+    }
+}
+} // namespace dev
+} // namespace mantiis

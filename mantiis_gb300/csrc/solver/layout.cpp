@@ -1,0 +1,390 @@
+#include "layout.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+
+#include "../boundary_tables.h"
+#include "../d2q9.h"
+
+namespace mantiis
+{
+namespace
+{
+// Node slopes of the three-node cubic spline with parabolically terminated
+// ends (the end intervals are parabolas): closed-form solution of
+//   d0 + d1 = 2 s0,  d0/h0 + 2 (1/h0 + 1/h1) d1 + d2/h1 = 3 (s0/h0 + s1/h1),  d1 + d2 = 2 s1
+// with s = secant slopes.
+void slopes3(const double t[3], const double v[3], double d[3])
+{
+    double h0 = t[1] - t[0], h1 = t[2] - t[1];
+    double s0 = (v[1] - v[0]) / h0, s1 = (v[2] - v[1]) / h1;
+    double r0 = 2 * s0, r2 = 2 * s1, r1 = 3 * (s0 / h0 + s1 / h1);
+    d[1] = (r1 - r0 / h0 - r2 / h1) / (1 / h0 + 1 / h1);
+    d[0] = r0 - d[1];
+    d[2] = r2 - d[1];
+}
+
+// Bicubic Hermite evaluation on the 3 (x) by 2 (y) node grid; F[j][i] at
+// (x[i], y[j]); x and y ascending.  Node slopes: 3-node spline along x,
+// straight line along y (a 2-node spline with parabolic ends is a line).
+double bicubic32(const double x[3], const double y[2], const double F[2][3], double qx, double qy)
+{
+    double Fx[2][3], Fy[2][3], Fxy[2][3];
+    for (int j = 0; j < 2; j++) slopes3(x, F[j], Fx[j]);
+    for (int i = 0; i < 3; i++)
+    {
+        double sy = (F[1][i] - F[0][i]) / (y[1] - y[0]);
+        Fy[0][i] = Fy[1][i] = sy;
+        double sxy = (Fx[1][i] - Fx[0][i]) / (y[1] - y[0]);
+        Fxy[0][i] = Fxy[1][i] = sxy;
+    }
+    // cell search clamped to the first/last interval (points outside extrapolate)
+    int ix = (qx <= x[1]) ? 0 : 1;
+    double hx = x[ix + 1] - x[ix], hy = y[1] - y[0];
+    double t = (qx - x[ix]) / hx, u = (qy - y[0]) / hy;
+    auto h00 = [](double s) { return 2 * s * s * s - 3 * s * s + 1; };
+    auto h01 = [](double s) { return -2 * s * s * s + 3 * s * s; };
+    auto g00 = [](double s) { return s * s * s - 2 * s * s + s; };
+    auto g01 = [](double s) { return s * s * s - s * s; };
+    double Hx[2] = {h00(t), h01(t)}, Gx[2] = {g00(t) * hx, g01(t) * hx};
+    double Hy[2] = {h00(u), h01(u)}, Gy[2] = {g00(u) * hy, g01(u) * hy};
+    double v = 0;
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+        {
+            int i = ix + a;
+            v += Hx[a] * Hy[b] * F[b][i] + Gx[a] * Hy[b] * Fx[b][i] + Hx[a] * Gy[b] * Fy[b][i] +
+                 Gx[a] * Gy[b] * Fxy[b][i];
+        }
+    return v;
+}
+
+int tiles_of(int W) { return (W + 31) / 32; }
+} // namespace
+
+void spline_weights(const double xin[3], const double yin[2], double qx, double qy, double w[6])
+{
+    // sort nodes ascending, remembering where each input node went
+    int px[3] = {0, 1, 2}, py[2] = {0, 1};
+    std::sort(px, px + 3, [&](int a, int b) { return xin[a] < xin[b]; });
+    if (yin[1] < yin[0]) std::swap(py[0], py[1]);
+    double x[3] = {xin[px[0]], xin[px[1]], xin[px[2]]}, y[2] = {yin[py[0]], yin[py[1]]};
+    for (int k = 0; k < 6; k++)
+    {
+        double F[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        int i = k % 3, j = k / 3; // input node (x index i, y index j) carries the unit value
+        int si = (int)(std::find(px, px + 3, i) - px), sj = (py[0] == j) ? 0 : 1;
+        F[sj][si] = 1.0;
+        w[k] = bicubic32(x, y, F, qx, qy);
+    }
+}
+
+ImageLayout build_layout(const Grid &g, const LayoutParams &p)
+{
+    using namespace d2q9;
+    ImageLayout L;
+    L.n = g.n;
+    L.max_level = g.max_level;
+    const int ML = g.max_level;
+    L.levels.resize(ML);
+    for (int l = 1; l <= ML; l++)
+    {
+        LevelLayout &lv = L.levels[l - 1];
+        lv.level = l;
+        lv.W = lv.H = g.n >> (l - 1);
+        lv.pitch = ((lv.W + 31) / 32) * 32;
+        lv.plane = (int64_t)lv.pitch * lv.H;
+        lv.tau.assign((size_t)lv.plane, 0.0f);
+        lv.spec.assign((size_t)lv.plane, 0u);
+        lv.substeps = 1 << (ML - l);
+        lv.snapshot_all = g.multiblock;
+        lv.tiles_x = tiles_of(lv.W);
+        lv.tiles_y = (lv.H + 7) / 8;
+    }
+    const int64_t N = g.n_cells;
+    L.cell_level.resize(N);
+    L.cell_site.resize(N);
+    for (int64_t c = 0; c < N; c++)
+    {
+        int l = g.level[c];
+        const LevelLayout &lv = L.levels[l - 1];
+        int sx = g.x[c] >> (l - 1), sy = g.y[c] >> (l - 1);
+        L.cell_level[c] = l;
+        L.cell_site[c] = sy * lv.pitch + sx;
+    }
+    auto torus_site = [&](int64_t c, int q) {
+        int l = g.level[c];
+        const LevelLayout &lv = L.levels[l - 1];
+        int sx = (g.x[c] >> (l - 1)) + CX[q], sy = (g.y[c] >> (l - 1)) + CY[q];
+        sx = (sx + lv.W) % lv.W;
+        sy = (sy + lv.H) % lv.H;
+        return sy * lv.pitch + sx;
+    };
+
+    // masks from the reference link lists
+    std::vector<uint32_t> arrive(N, 0), over(N, 0), wall(N, 0), quirk(N, 0);
+    for (size_t k = 0; k < g.stream_id.size(); k++)
+    {
+        int64_t src = g.stream_id[k], dst = g.stream_loc[k];
+        int q = g.stream_ic[k];
+        if (torus_site(src, q) != L.cell_site[dst] || g.level[src] != g.level[dst])
+            throw std::runtime_error("layout: stream link does not land on its torus neighbour");
+        arrive[dst] |= 1u << q;
+    }
+    for (size_t k = 0; k < g.per_id.size(); k++)
+    {
+        int64_t src = g.per_id[k], dst = g.per_i2[k];
+        int q = g.per_ic[k];
+        if (torus_site(src, q) != L.cell_site[dst] || g.level[src] != g.level[dst])
+            throw std::runtime_error("layout: periodic link does not land on its torus neighbour");
+        arrive[dst] |= 1u << q;
+        over[dst] |= 1u << q;
+    }
+    for (size_t k = 0; k < g.wall_id.size(); k++)
+    {
+        int64_t c = g.wall_id[k];
+        int q = g.wall_ic[k];
+        wall[c] |= 1u << q;
+        if (g.conn[(size_t)c * 9 + q] >= 0) quirk[c] |= 1u << q;
+    }
+
+    // interpolation buffer targets
+    std::vector<int32_t> buf_of(N, -1);
+    auto want_buf = [&](int64_t c) {
+        if (c < 0) return;
+        if (buf_of[c] < 0)
+        {
+            buf_of[c] = (int32_t)L.n_buffers++;
+            L.buf_level.push_back(g.level[c]);
+            L.buf_site.push_back(L.cell_site[c]);
+        }
+    };
+    for (auto &row : g.coarse_rows)
+        if (row[0] >= 0 && g.is_buffer[row[0]]) want_buf(row[0]);
+    for (auto &row : g.fine_rows)
+        for (int k = 1; k < 5; k++)
+            if (row[k] >= 0 && g.is_buffer[row[k]]) want_buf(row[k]);
+
+    const uint32_t ALL = 0x1FFu;
+    for (int64_t c = 0; c < N; c++)
+    {
+        int l = g.level[c];
+        LevelLayout &lv = L.levels[l - 1];
+        int s = L.cell_site[c];
+        if (lv.tau[(size_t)s] != 0.0f) throw std::runtime_error("layout: two cells share a site");
+        float tau = (float)g.tau[c];
+        if (!(tau > 0.0f)) throw std::runtime_error("layout: non-positive relaxation time");
+        uint32_t flags = 0;
+        if (buf_of[c] >= 0) flags |= SF_BUFFER;
+        if (p.adsorption && c == g.inlet && g.outlet >= 0) flags |= SF_INLET;
+        if (p.adsorption && c == g.outlet && g.inlet >= 0) flags |= SF_OUTLET;
+        bool special = arrive[c] != ALL || wall[c] != 0 || flags != 0;
+        lv.n_active++;
+        if (!g.is_buffer[c]) lv.n_active_real++;
+        if (!special)
+        {
+            lv.tau[(size_t)s] = tau;
+            continue;
+        }
+        SpecialRec rec{};
+        int b = g.bnd[c];
+        rec.m0 = arrive[c] | (over[c] << 9) | (wall[c] << 18);
+        rec.m1 = quirk[c] | ((uint32_t)(b < 0 ? 0xFF : b) << 9) | (flags << 17);
+        double kn = g.kn[c];
+        double r = 0.0;
+        if (wall[c])
+        {
+            if (p.wall == WALL_SRBB) r = 0.4987 * std::pow(kn, -0.131) - 0.25;
+            else if (p.wall == WALL_MDBB) r = 0.3222 * std::pow(kn, -0.217) - 0.25;
+        }
+        rec.r = (float)r;
+        rec.quirk_base = -1;
+        if (quirk[c])
+        {
+            rec.quirk_base = (int32_t)L.n_quirk;
+            L.n_quirk += __builtin_popcount(quirk[c]);
+        }
+        rec.buf = buf_of[c];
+        // constant part of each population's deviation: rho0 * K_p
+        double K[9] = {0};
+        for (int q = 0; q < 9; q++)
+            if (!((arrive[c] >> q) & 1)) K[q] -= W[q];
+        if (p.wall == WALL_SRBB)
+        {
+            for (int q = 0; q < 9; q++)
+            {
+                if (!((wall[c] >> q) & 1)) continue;
+                int p1 = OPP[q];
+                int p2 = (b >= 0) ? MANTIIS_ICSR[b][q] : OPP[q];
+                if (!((over[c] >> p1) & 1)) K[p1] += r * W[q];
+                if (!((over[c] >> p2) & 1)) K[p2] += (1 - r) * W[q];
+            }
+        }
+        else
+        {
+            // BB / MDBB assign the reflected population outright
+            for (int q = 0; q < 9; q++)
+                if (((wall[c] >> q) & 1) && !((over[c] >> OPP[q]) & 1)) K[OPP[q]] = 0.0;
+        }
+        bool hasK = false;
+        for (int q = 0; q < 9; q++)
+            if (std::fabs(K[q]) > 1e-15) hasK = true;
+        rec.k_row = -1;
+        if (hasK)
+        {
+            rec.k_row = (int32_t)(L.ktab.size() / 9);
+            for (int q = 0; q < 9; q++) L.ktab.push_back((float)(p.rho0 * K[q]));
+            rec.m1 |= (uint32_t)SF_HAS_K << 17;
+        }
+        lv.tau[(size_t)s] = -tau;
+        lv.spec[(size_t)s] = (uint32_t)L.specials.size();
+        L.specials.push_back(rec);
+    }
+
+    // active tiles (32 x 8 sites)
+    for (auto &lv : L.levels)
+    {
+        for (int ty = 0; ty < lv.tiles_y; ty++)
+            for (int tx = 0; tx < lv.tiles_x; tx++)
+            {
+                bool any = false;
+                for (int yy = ty * 8; yy < std::min(lv.H, ty * 8 + 8) && !any; yy++)
+                    for (int xx = tx * 32; xx < std::min(lv.W, tx * 32 + 32); xx++)
+                        if (lv.tau[(size_t)yy * lv.pitch + xx] != 0.0f)
+                        {
+                            any = true;
+                            break;
+                        }
+                if (any) lv.tile_list.push_back(ty * lv.tiles_x + tx);
+            }
+    }
+
+    // interfaces (include/coreLB.hpp:1101-1231)
+    auto is_coarse_buffer = [&](int64_t c) { return g.is_buffer[c] && g.type[c] == 10 * g.level[c] + g.level[c] - 1; };
+    for (int l1 = 1; l1 < ML; l1++)
+    {
+        int l2 = l1 + 1;
+        InterfaceLayout itf;
+        itf.l1 = l1;
+        itf.l2 = l2;
+        int ckey = 10 * l2 + l1, fkey = 10 * l1 + l2;
+        for (size_t r = 0; r < g.coarse_rows.size(); r++)
+        {
+            if (g.coarse_key[r] != ckey) continue;
+            const auto &row = g.coarse_rows[r];
+            if (row[0] < 0 || buf_of[row[0]] < 0) continue;
+            CoarseRowDev d{};
+            d.site = L.cell_site[row[0]];
+            d.buf = buf_of[row[0]];
+            double tsum = 0;
+            int cnt = 0;
+            for (int k = 0; k < 4; k++)
+            {
+                int64_t ch = row[k + 1];
+                d.child[k] = ch >= 0 ? L.cell_site[ch] : -1;
+                d.child_buf[k] = (ch >= 0 && is_coarse_buffer(ch) && g.level[ch] <= l2) ? buf_of[ch] : -1;
+                if (ch >= 0)
+                {
+                    tsum += g.tau[ch];
+                    cnt++;
+                }
+            }
+            if (cnt == 0) continue;
+            d.ratio = (float)(2 * g.tau[row[0]] / (tsum / cnt));
+            d.inv_nchild = 1.0f / cnt;
+            itf.coarse.push_back(d);
+        }
+        const int top_order[9] = {7, 4, 8, 3, 0, 1, 6, 2, 5};
+        const int bottom_order[9] = {6, 2, 5, 3, 0, 1, 7, 4, 8};
+        double parent_shift = std::pow(2.0, l2 - 2) - 0.5;
+        double child_shift = (l1 == 1) ? 0 : std::pow(2.0, l1 - 2) - 0.5;
+        for (size_t r = 0; r < g.fine_rows.size(); r++)
+        {
+            if (g.fine_key[r] != fkey) continue;
+            const auto &row = g.fine_rows[r];
+            int64_t pc = row[0];
+            int lvp = g.level[pc];
+            int thr = 1 << (lvp - 1);
+            double X[9], Y[9];
+            int64_t nb_cell[9];
+            for (int q = 0; q < 9; q++)
+            {
+                int64_t nb = g.conn[(size_t)pc * 9 + q];
+                nb_cell[q] = nb;
+                if (nb < 0)
+                {
+                    // wall / missing neighbour: nominal lattice position, parent's value
+                    X[q] = g.y[pc] + CY[q] * thr + parent_shift + 1;
+                    Y[q] = g.x[pc] + CX[q] * thr + parent_shift + 1;
+                    continue;
+                }
+                int dy = g.y[pc] - g.y[nb], dxv = g.x[pc] - g.x[nb];
+                if (std::abs(dy) > thr && dy < 0) X[q] = g.y[pc] + parent_shift + 1 - 2;
+                else if (std::abs(dy) > thr && dy > 0) X[q] = g.y[pc] + parent_shift + 1 + 2;
+                else X[q] = g.y[nb] + parent_shift + 1;
+                if (std::abs(dxv) > thr && dxv < 0) Y[q] = g.x[pc] + parent_shift + 1 - 2;
+                else if (std::abs(dxv) > thr && dxv > 0) Y[q] = g.x[pc] + parent_shift + 1 + 2;
+                else Y[q] = g.x[nb] + parent_shift + 1;
+            }
+            std::vector<double> xs(X, X + 9), ys(Y, Y + 9);
+            std::sort(xs.begin(), xs.end());
+            xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+            std::sort(ys.begin(), ys.end());
+            ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
+            if (xs.size() != 3 || ys.size() != 3) throw std::runtime_error("layout: spline nodes are not a 3x3 lattice");
+            bool top = g.y[pc] < g.n / 2;
+            double ynode[2] = {top ? xs[0] : xs[2], xs[1]};
+            double xnode[3] = {ys[0], ys[1], ys[2]};
+            const int *order = top ? top_order : bottom_order;
+            FineRowDev d{};
+            for (int k = 0; k < 6; k++)
+            {
+                int64_t nb = nb_cell[order[k]];
+                int64_t src = nb >= 0 ? nb : pc;
+                d.node_site[k] = L.cell_site[src];
+                d.node_buf[k] = (is_coarse_buffer(src) && g.level[src] <= l2) ? buf_of[src] : -1;
+            }
+            for (int k = 0; k < 4; k++)
+            {
+                int64_t ch = row[k + 1];
+                d.child_site[k] = L.cell_site[ch];
+                d.child_buf[k] = buf_of[ch];
+                double w[6];
+                spline_weights(xnode, ynode, g.x[ch] + child_shift + 1, g.y[ch] + child_shift + 1, w);
+                double sum = 0;
+                for (int j = 0; j < 6; j++)
+                {
+                    d.weight[k][j] = (float)w[j];
+                    sum += w[j];
+                }
+                if (std::fabs(sum - 1.0) > 1e-9) throw std::runtime_error("layout: spline weights do not sum to one");
+                d.ratio[k] = (float)(g.tau[ch] / (2 * g.tau[pc]));
+            }
+            itf.fine.push_back(d);
+        }
+        L.interfaces.push_back(std::move(itf));
+    }
+
+    // statistics: mean tau, pixel area, lattice updates per coarse step
+    double ts = 0;
+    int64_t nt = 0;
+    for (int64_t c = 0; c < N; c++)
+    {
+        int l = g.level[c];
+        double lu = (double)(1 << (ML - l));
+        if (g.is_buffer[c])
+        {
+            L.buffer_lu_per_coarse_step += lu;
+            continue;
+        }
+        ts += g.tau[c];
+        nt++;
+        L.pixel_area_cells += (int64_t)1 << (2 * (l - 1));
+        L.lu_per_coarse_step += lu;
+    }
+    L.tau_mean = nt ? ts / nt : 0.0;
+    return L;
+}
+} // namespace mantiis

@@ -1,0 +1,954 @@
+// Host context of the GB300 lattice Boltzmann solver and its C ABI
+// (include/mantiis_gpu.h).  One context = one pore image on one GPU stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/mantiis_gpu.h"
+#include "../boundary_tables.h"
+#include "../host/geometry.hpp"
+#include "../host/grid.hpp"
+#include "../host/units.hpp"
+#include "kernels.cuh"
+#include "layout.hpp"
+
+using namespace mantiis;
+
+namespace
+{
+thread_local std::string g_error;
+
+struct CudaError : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+struct InputError : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+
+#define CK(call)                                                                                                       \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess)                                                                                         \
+            throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + __FILE__ + ":" +              \
+                            std::to_string(__LINE__) + ")");                                                           \
+    } while (0)
+
+template <typename T> struct DevBuf
+{
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n)
+    {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o)
+        {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count, int64_t &acct)
+    {
+        release();
+        if (count == 0) return;
+        CK(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+        acct += (int64_t)(count * sizeof(T));
+    }
+    void upload(const std::vector<T> &v, int64_t &acct, cudaStream_t s)
+    {
+        alloc(v.size(), acct);
+        if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void zero(cudaStream_t s)
+    {
+        if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+struct LevelDev
+{
+    DevBuf<float> f, tau, tau2, snap, unorm;
+    DevBuf<uint32_t> spec;
+    DevBuf<int32_t> tiles;
+    int64_t steps = 0; // substeps done at this level
+};
+
+struct InterfaceDev
+{
+    DevBuf<CoarseRowDev> coarse;
+    DevBuf<FineRowDev> fine;
+    int l1 = 1;
+    int ncoarse = 0, nfine = 0;
+};
+
+constexpr int kRing = 8192; // residual accumulator slots (4 doubles each)
+
+} // namespace
+
+struct mgpu_ctx
+{
+    mgpu_params prm{};
+    UnitSystem units;
+    Grid grid;
+    ImageLayout lay;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t bytes = 0;
+    int64_t launches = 0;
+    std::string err;
+
+    std::vector<LevelDev> lv;
+    std::vector<InterfaceDev> itf;
+    DevBuf<SpecialRec> specials;
+    DevBuf<float> ktab, side, ibuf;
+    DevBuf<int32_t> cell_level, cell_site;
+    DevBuf<double> red;     // kRing * 4
+    DevBuf<double> out_rho, out_ux, out_uy, out_f;
+    DevBuf<unsigned int> errword;
+    float rho0f = 0.f;
+
+    cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
+    int64_t graph_launches = 0;
+    int64_t coarse_done = 0;     // coarse steps executed since creation
+    int64_t ref_t = 0;           // reference lb->t
+    std::vector<double> residuals;
+    bool stored_u_valid = false; // |u| of the current state has been stored
+
+    // checkpoint of the mutable state (exact break semantics)
+    struct Checkpoint
+    {
+        std::vector<std::unique_ptr<DevBuf<float>>> f;
+        DevBuf<float> ibuf, side;
+        std::vector<std::unique_ptr<DevBuf<float>>> unorm;
+        std::vector<int64_t> steps;
+        int64_t coarse_done = 0;
+        bool valid = false;
+    } ckpt;
+
+    dev::Common common() const
+    {
+        dev::Common C{};
+        C.specials = specials.p;
+        C.ktab = ktab.p;
+        C.side = side.p;
+        C.n_quirk = lay.n_quirk;
+        C.ibuf = ibuf.p;
+        C.n_buf = lay.n_buffers;
+        C.rho0 = rho0f;
+        C.inlet_axis = (float)(d2q9::W[1] * units.rhoin - d2q9::W[1] * (double)rho0f);
+        C.inlet_diag = (float)(d2q9::W[2] * units.rhoin - d2q9::W[5] * (double)rho0f);
+        C.wall = prm.wall;
+        C.collision = prm.collision;
+        C.fbody = (float)prm.fbody;
+        C.psi_form = prm.psi_form;
+        C.psi_rho0 = (float)prm.rho_psi;
+        C.eos_a = (float)units.a_alpha_lu;
+        C.eos_b = (float)UnitSystem::b_lu;
+        C.eos_T = (float)units.T_lu;
+        C.g_ff = (float)prm.g_ff;
+        C.g_fs = (float)prm.g_fs;
+        C.red = red.p;
+        C.err = errword.p;
+        return C;
+    }
+    dev::LevelView view(int l) const
+    {
+        const LevelLayout &ll = lay.levels[l];
+        const LevelDev &d = lv[l];
+        dev::LevelView v{};
+        v.f = d.f.p;
+        v.tau = d.tau.p;
+        v.spec = d.spec.p;
+        v.tau2 = d.tau2.p;
+        v.snap = d.snap.p;
+        v.unorm = d.unorm.p;
+        v.tiles = d.tiles.p;
+        v.ntiles = (int)ll.tile_list.size();
+        v.tiles_x = ll.tiles_x;
+        v.W = ll.W;
+        v.H = ll.H;
+        v.pitch = ll.pitch;
+        v.plane = ll.plane;
+        v.fshift = (float)(prm.fbody / 2.0 * std::pow(2.0, l));
+        v.level = l + 1;
+        return v;
+    }
+    dev::AllLevels all() const
+    {
+        dev::AllLevels A{};
+        for (int l = 0; l < (int)lv.size(); l++)
+        {
+            A.lv[l] = view(l);
+            A.parity[l] = (int)(lv[l].steps & 1);
+            A.direct[l] = lv[l].steps == 0 ? 1 : 0;
+        }
+        return A;
+    }
+};
+
+namespace
+{
+int fail(mgpu_ctx *ctx, int code, const std::string &msg)
+{
+    g_error = msg;
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+template <typename F> int guarded(mgpu_ctx *ctx, F &&fn)
+{
+    try
+    {
+        return fn();
+    }
+    catch (const CudaError &e)
+    {
+        return fail(ctx, MGPU_E_CUDA, e.what());
+    }
+    catch (const InputError &e)
+    {
+        return fail(ctx, MGPU_E_INPUT, e.what());
+    }
+    catch (const std::invalid_argument &e)
+    {
+        return fail(ctx, MGPU_E_INPUT, e.what());
+    }
+    catch (const std::runtime_error &e)
+    {
+        std::string m = e.what();
+        bool input = m.rfind("[ERROR]", 0) == 0;
+        return fail(ctx, input ? MGPU_E_INPUT : MGPU_E_ARG, m);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(ctx, MGPU_E_ARG, e.what());
+    }
+}
+
+void upload_constants()
+{
+    unsigned char icsr[MANTIIS_N_BND_TYPES * 9];
+    unsigned short npos[MANTIIS_N_BND_TYPES], nneg[MANTIIS_N_BND_TYPES];
+    for (int t = 0; t < MANTIIS_N_BND_TYPES; t++)
+    {
+        npos[t] = nneg[t] = 0;
+        for (int q = 0; q < 9; q++)
+        {
+            icsr[t * 9 + q] = MANTIIS_ICSR[t][q];
+            double cn = d2q9::CY[q] * MANTIIS_XY_NORM[t][1] + d2q9::CX[q] * MANTIIS_XY_NORM[t][0];
+            if (cn > 0) npos[t] |= (unsigned short)(1u << q);
+            else if (cn < 0) nneg[t] |= (unsigned short)(1u << q);
+        }
+    }
+    CK(cudaMemcpyToSymbol(dev::c_icsr, icsr, sizeof(icsr)));
+    CK(cudaMemcpyToSymbol(dev::c_npos, npos, sizeof(npos)));
+    CK(cudaMemcpyToSymbol(dev::c_nneg, nneg, sizeof(nneg)));
+}
+
+void launch_check(mgpu_ctx *ctx)
+{
+    ctx->launches++;
+    CK(cudaGetLastError());
+}
+
+// ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
+void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
+{
+    const int L = ctx->lay.max_level;
+    dev::Common C = ctx->common();
+    const bool mb = ctx->grid.multiblock;
+    for (int l = L - 1; l >= 0; l--)
+    {
+        LevelLayout &ll = ctx->lay.levels[l];
+        if (ll.tile_list.empty())
+        {
+            ctx->lv[l].steps += ll.substeps;
+            continue;
+        }
+        for (int sub = 0; sub < ll.substeps; sub++)
+        {
+            dev::LevelView V = ctx->view(l);
+            dev::StepOpt o{};
+            o.parity = (int)(ctx->lv[l].steps & 1);
+            o.direct = ctx->lv[l].steps == 0 ? 1 : 0;
+            o.first_sub = sub == 0;
+            o.snap_store = mb && sub == 0;
+            o.snap_use = mb && sub > 0;
+            o.diff = (sub == 0 && diff) ? 1 : 0;
+            o.store_u = (sub == 0 && store_u) ? 1 : 0;
+            o.red_slot = red_slot;
+            dim3 grid((unsigned)ll.tile_list.size()), block(256);
+            if (o.parity == 0) dev::k_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            launch_check(ctx);
+            ctx->lv[l].steps++;
+        }
+    }
+    // interface exchange, finest first (include/coreLB.hpp:1327-1330)
+    for (auto &it : ctx->itf)
+    {
+        int l1 = it.l1 - 1, l2 = it.l1;
+        dev::LevelView Vf = ctx->view(l1), Vc = ctx->view(l2);
+        int pf = (int)(ctx->lv[l1].steps & 1), pc = (int)(ctx->lv[l2].steps & 1);
+        if (it.ncoarse)
+        {
+            dim3 grid((it.ncoarse + 127) / 128), block(128);
+            if (pf == 0) dev::k_coarse<0><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.coarse.p, it.ncoarse);
+            else dev::k_coarse<1><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.coarse.p, it.ncoarse);
+            launch_check(ctx);
+        }
+        if (it.nfine)
+        {
+            dim3 grid((it.nfine + 127) / 128), block(128);
+            if (pc == 0) dev::k_fine<0><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.fine.p, it.nfine);
+            else dev::k_fine<1><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.fine.p, it.nfine);
+            launch_check(ctx);
+        }
+    }
+    ctx->coarse_done++;
+}
+
+// read pass over all reference cells
+void cells_pass(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f, bool diff, bool store_u, int red_slot)
+{
+    int64_t n = ctx->grid.n_cells;
+    if (n == 0) return;
+    dim3 grid((unsigned)((n + 255) / 256)), block(256);
+    dev::k_cells<<<grid, block, 0, ctx->stream>>>(ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, rho,
+                                                   ux, uy, f, diff ? 1 : 0, store_u ? 1 : 0, red_slot);
+    launch_check(ctx);
+}
+
+void zero_slots(mgpu_ctx *ctx, int first, int count)
+{
+    // slots are used cyclically; zero a contiguous (possibly wrapping) range
+    for (int k = 0; k < count; k++)
+    {
+        int s = (first + k) % kRing;
+        CK(cudaMemsetAsync(ctx->red.p + (size_t)s * 4, 0, 4 * sizeof(double), ctx->stream));
+    }
+}
+
+void read_slot(mgpu_ctx *ctx, int slot, double out[4])
+{
+    CK(cudaMemcpyAsync(out, ctx->red.p + (size_t)(slot % kRing) * 4, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+}
+
+void checkpoint_save(mgpu_ctx *ctx)
+{
+    auto &k = ctx->ckpt;
+    int64_t dummy = 0;
+    if (!k.valid && k.f.empty())
+    {
+        for (auto &l : ctx->lv)
+        {
+            k.f.emplace_back(new DevBuf<float>());
+            k.f.back()->alloc(l.f.n, dummy);
+            k.unorm.emplace_back(new DevBuf<float>());
+            k.unorm.back()->alloc(l.unorm.n, dummy);
+        }
+        k.ibuf.alloc(ctx->ibuf.n, dummy);
+        k.side.alloc(ctx->side.n, dummy);
+        ctx->bytes += dummy;
+    }
+    for (size_t l = 0; l < ctx->lv.size(); l++)
+    {
+        if (ctx->lv[l].f.n)
+            CK(cudaMemcpyAsync(k.f[l]->p, ctx->lv[l].f.p, ctx->lv[l].f.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (ctx->lv[l].unorm.n)
+            CK(cudaMemcpyAsync(k.unorm[l]->p, ctx->lv[l].unorm.p, ctx->lv[l].unorm.n * 4, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+    }
+    if (ctx->ibuf.n) CK(cudaMemcpyAsync(k.ibuf.p, ctx->ibuf.p, ctx->ibuf.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ctx->side.n) CK(cudaMemcpyAsync(k.side.p, ctx->side.p, ctx->side.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    k.steps.clear();
+    for (auto &l : ctx->lv) k.steps.push_back(l.steps);
+    k.coarse_done = ctx->coarse_done;
+    k.valid = true;
+}
+
+void checkpoint_restore(mgpu_ctx *ctx)
+{
+    auto &k = ctx->ckpt;
+    for (size_t l = 0; l < ctx->lv.size(); l++)
+    {
+        if (ctx->lv[l].f.n)
+            CK(cudaMemcpyAsync(ctx->lv[l].f.p, k.f[l]->p, ctx->lv[l].f.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (ctx->lv[l].unorm.n)
+            CK(cudaMemcpyAsync(ctx->lv[l].unorm.p, k.unorm[l]->p, ctx->lv[l].unorm.n * 4, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+        ctx->lv[l].steps = k.steps[l];
+    }
+    if (ctx->ibuf.n) CK(cudaMemcpyAsync(ctx->ibuf.p, k.ibuf.p, ctx->ibuf.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ctx->side.n) CK(cudaMemcpyAsync(ctx->side.p, k.side.p, ctx->side.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->coarse_done = k.coarse_done;
+}
+
+// Steps [k0+1 .. k0+n] with the residual of every step in slots (step index
+// mod kRing).  Kernel of step k reads state k-1, so it evaluates residual k-1;
+// the residual of the last step comes from a read pass.
+void run_batch_with_residuals(mgpu_ctx *ctx, int n)
+{
+    int64_t k0 = ctx->coarse_done;
+    zero_slots(ctx, (int)((k0 + 1) % kRing), n);
+    for (int i = 0; i < n; i++)
+    {
+        int64_t k = ctx->coarse_done + 1; // this step
+        bool diff = i > 0;                // residual of step k-1 (the previous batch closed its own last one)
+        int slot = (int)(((k - 1) % kRing) * 4);
+        coarse_step(ctx, diff, true, slot);
+    }
+    int64_t last = ctx->coarse_done;
+    cells_pass(ctx, nullptr, nullptr, nullptr, nullptr, true, false, (int)((last % kRing) * 4));
+}
+
+void transport_only(mgpu_ctx *ctx)
+{
+    if (ctx->prm.simulation != MGPU_SIM_TRANSPORT)
+        throw std::runtime_error("this build of the solver runs the transport simulation only");
+}
+} // namespace
+
+extern "C" {
+
+void mgpu_default_params(mgpu_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->simulation = MGPU_SIM_TRANSPORT;
+    p->collision = 2;
+    p->wall = 2;
+    p->multiblock = 0;
+    p->max_allowed_level = 2;
+    p->dx = 1.0e-9;
+    p->fbody = 1.0e-8;
+    p->T = 300.0;
+    p->P = 2.0e6;
+    p->tol = 1.0e-10;
+    p->psi_form = 0;
+    p->rho_psi = 1.0;
+    p->g_ff = -1.0;
+    p->g_fs = -12.7;
+    p->rho_init = 0.0;
+    p->rho_noise = 0.0;
+    p->seed = 0;
+    p->check_every = 1;
+}
+
+static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **out)
+{
+    if (!p || !out) throw std::invalid_argument("null argument");
+    if (p->collision < 0 || p->collision > 2)
+        throw std::runtime_error("Incorrect keyword for collision: available options are\n\t 2 for regularized MRT\n"
+                                 "\t 1 for simple MRT\n\t 0 for simple BGK\n");
+    if (p->wall < 0 || p->wall > 2)
+        throw std::runtime_error("Incorrect keyword for wall boundary method: available options are\n\t 2 for SRBBWall\n"
+                                 "\t 1 for MDBBWall\n\t 0 for BBWall\n");
+    if (p->simulation < 0 || p->simulation > 2) throw std::runtime_error("Unknown simulation type");
+    if (p->check_every < 1) throw std::invalid_argument("check_every must be >= 1");
+    std::unique_ptr<mgpu_ctx> ctx(new mgpu_ctx());
+    ctx->prm = *p;
+    ctx->units.Cl = p->dx;
+    ctx->units.T_phy = p->T;
+    ctx->units.P_phy = p->P;
+    ctx->units.recompute();
+    GridOptions go;
+    go.multiblock = p->multiblock != 0;
+    go.max_allowed_level = p->max_allowed_level;
+    go.dx = p->dx;
+    go.mfp = ctx->units.mfp;
+    ctx->grid = build_grid(img, go);
+    if (ctx->grid.max_level > dev::kMaxLevels) throw std::runtime_error("too many refinement levels");
+    transport_only(ctx.get());
+
+    double rho_init = p->rho_init > 0 ? p->rho_init : ctx->units.rhoin;
+    ctx->rho0f = (float)rho_init;
+    LayoutParams lp;
+    lp.wall = p->wall;
+    lp.collision = p->collision;
+    lp.rho0 = (double)ctx->rho0f;
+    lp.adsorption = p->simulation != MGPU_SIM_TRANSPORT;
+    ctx->lay = build_layout(ctx->grid, lp);
+
+    CK(cudaGetDevice(&ctx->device));
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    ctx->own_stream = true;
+    upload_constants();
+    cudaStream_t s = ctx->stream;
+    int64_t &acct = ctx->bytes;
+    ctx->lv.resize(ctx->lay.levels.size());
+    for (size_t l = 0; l < ctx->lv.size(); l++)
+    {
+        const LevelLayout &ll = ctx->lay.levels[l];
+        LevelDev &d = ctx->lv[l];
+        d.f.alloc((size_t)ll.plane * 9, acct);
+        d.f.zero(s);
+        d.tau.upload(ll.tau, acct, s);
+        d.spec.upload(ll.spec, acct, s);
+        d.tiles.upload(ll.tile_list, acct, s);
+        d.unorm.alloc((size_t)ll.plane, acct);
+        d.unorm.zero(s);
+        if (ll.snapshot_all)
+        {
+            d.snap.alloc((size_t)ll.plane * 3, acct);
+            d.snap.zero(s);
+        }
+    }
+    ctx->specials.upload(ctx->lay.specials, acct, s);
+    ctx->ktab.upload(ctx->lay.ktab, acct, s);
+    ctx->side.alloc((size_t)ctx->lay.n_quirk * 2, acct);
+    ctx->side.zero(s);
+    ctx->ibuf.alloc((size_t)ctx->lay.n_buffers * 9, acct);
+    ctx->ibuf.zero(s);
+    ctx->cell_level.upload(ctx->lay.cell_level, acct, s);
+    ctx->cell_site.upload(ctx->lay.cell_site, acct, s);
+    ctx->red.alloc((size_t)kRing * 4, acct);
+    ctx->red.zero(s);
+    ctx->errword.alloc(1, acct);
+    ctx->errword.zero(s);
+    for (auto &it : ctx->lay.interfaces)
+    {
+        ctx->itf.emplace_back();
+        InterfaceDev &e = ctx->itf.back();
+        e.l1 = it.l1;
+        e.ncoarse = (int)it.coarse.size();
+        e.nfine = (int)it.fine.size();
+        e.coarse.upload(it.coarse, acct, s);
+        e.fine.upload(it.fine, acct, s);
+    }
+
+    // initial state: rho = rho_init, u = 0, f = f_eq (include/coreLB.hpp:381-417)
+    std::vector<double> rho(ctx->grid.n_cells, rho_init), zero(ctx->grid.n_cells, 0.0);
+    if (p->rho_noise > 0)
+    {
+        std::mt19937_64 rng(p->seed);
+        std::uniform_real_distribution<double> u(-p->rho_noise, p->rho_noise);
+        for (auto &v : rho) v += u(rng);
+    }
+    DevBuf<double> dr, du, dv;
+    int64_t tmp = 0;
+    dr.upload(rho, tmp, s);
+    du.upload(zero, tmp, s);
+    dv.upload(zero, tmp, s);
+    int64_t n = ctx->grid.n_cells;
+    if (n > 0)
+    {
+        dev::k_set_equilibrium<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ctx->all(), ctx->common(), ctx->cell_level.p,
+                                                                          ctx->cell_site.p, n, dr.p, du.p, dv.p);
+        launch_check(ctx.get());
+    }
+    CK(cudaStreamSynchronize(s));
+    *out = ctx.release();
+    return MGPU_OK;
+}
+
+int mgpu_create(const int32_t *pore, const double *kn, const double *locpore, int n, const mgpu_params *p, mgpu_ctx **out)
+{
+    return guarded(nullptr, [&]() {
+        if (!pore || !kn || !locpore || n <= 0) throw std::invalid_argument("null image or bad size");
+        PoreImage img;
+        img.n = n;
+        img.pore.assign(pore, pore + (size_t)n * n);
+        img.kn.assign(kn, kn + (size_t)n * n);
+        img.locpore.assign(locpore, locpore + (size_t)n * n);
+        return create_impl(img, p, out);
+    });
+}
+
+int mgpu_create_from_folder(const char *folder, int n, const mgpu_params *p, mgpu_ctx **out)
+{
+    return guarded(nullptr, [&]() {
+        if (!folder) throw std::invalid_argument("null folder");
+        PoreImage img = load_pore_image(folder, n);
+        return create_impl(img, p, out);
+    });
+}
+
+int mgpu_destroy(mgpu_ctx *ctx)
+{
+    if (!ctx) return MGPU_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MGPU_OK;
+}
+
+int mgpu_get_info(const mgpu_ctx *ctx, mgpu_info *info)
+{
+    if (!ctx || !info) return fail(nullptr, MGPU_E_ARG, "null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->n = ctx->grid.n;
+    info->max_level = ctx->grid.max_level;
+    info->n_cells = ctx->grid.n_cells;
+    int64_t nb = 0;
+    for (auto v : ctx->grid.is_buffer) nb += v;
+    info->n_buffer_cells = nb;
+    info->n_special = (int64_t)ctx->lay.specials.size();
+    info->lu_per_step = ctx->lay.lu_per_coarse_step;
+    info->buffer_lu_per_step = ctx->lay.buffer_lu_per_coarse_step;
+    info->rho_in = ctx->units.rhoin;
+    info->mfp = ctx->units.mfp;
+    info->tau_mean = ctx->lay.tau_mean;
+    info->device_bytes = ctx->bytes;
+    const GridDiagnostics &d = ctx->grid.diag;
+    info->grid_undefined_cases =
+        d.buffer_wall_links + d.fine_parent_missing_nbr + d.coarse_missing_child + d.fine_group_unmatched + d.pore_search_failed;
+    return MGPU_OK;
+}
+
+int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || n_steps < 0) throw std::invalid_argument("bad argument");
+        const double tol = ctx->prm.tol;
+        const int batch_max = 1000;
+        int done = 0;
+        bool broke = false;
+        while (done < n_steps && !broke)
+        {
+            int batch = std::min(batch_max, n_steps - done);
+            checkpoint_save(ctx);
+            int64_t k0 = ctx->coarse_done;
+            run_batch_with_residuals(ctx, batch);
+            std::vector<double> slots((size_t)batch * 4);
+            for (int i = 0; i < batch; i++) read_slot(ctx, (int)((k0 + 1 + i) % kRing), &slots[(size_t)i * 4]);
+            CK(cudaStreamSynchronize(ctx->stream));
+            int stop = -1;
+            for (int i = 0; i < batch; i++)
+            {
+                double d = slots[(size_t)i * 4] / slots[(size_t)i * 4 + 1];
+                ctx->residuals.push_back(d);
+                if (d < tol)
+                {
+                    stop = i;
+                    break;
+                }
+            }
+            if (stop >= 0)
+            {
+                // the reference stops right after this step: replay up to it
+                if (stop + 1 < batch)
+                {
+                    checkpoint_restore(ctx);
+                    for (int i = 0; i <= stop; i++) coarse_step(ctx, false, true, 0);
+                }
+                done += stop + 1;
+                ctx->ref_t += stop; // the breaking step is not counted (include/mantiisApp.hpp:302-350)
+                broke = true;
+            }
+            else
+            {
+                done += batch;
+                ctx->ref_t += batch;
+            }
+        }
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (steps_done) *steps_done = done;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_advance(mgpu_ctx *ctx, int n_steps)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || n_steps < 0) throw std::invalid_argument("bad argument");
+        const int K = ctx->prm.check_every;
+        std::vector<int64_t> pending;
+        auto flush = [&]() {
+            if (pending.empty()) return;
+            std::vector<double> v(pending.size() * 4);
+            for (size_t i = 0; i < pending.size(); i++) read_slot(ctx, (int)pending[i], &v[i * 4]);
+            CK(cudaStreamSynchronize(ctx->stream));
+            for (size_t i = 0; i < pending.size(); i++) ctx->residuals.push_back(v[i * 4] / v[i * 4 + 1]);
+            pending.clear();
+        };
+        for (int i = 0; i < n_steps; i++)
+        {
+            int64_t k = ctx->coarse_done + 1;
+            // residual of step s is evaluated by kernel s+1 against |u| stored by kernel s
+            bool diff = k >= 2 && ((k - 1) % K == 0);
+            bool store = (k % K == 0);
+            int slot = (int)(((k - 1) % kRing) * 4);
+            if (diff) zero_slots(ctx, (int)((k - 1) % kRing), 1);
+            coarse_step(ctx, diff, store, slot);
+            if (diff) pending.push_back(k - 1);
+            if ((int)pending.size() >= kRing / 2) flush();
+        }
+        flush();
+        ctx->ref_t += n_steps;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || n_steps < 0) throw std::invalid_argument("bad argument");
+        int left = n_steps;
+        // the graph starts from a stepped state (not the initial "direct" one)
+        bool fresh = false;
+        for (auto &l : ctx->lv) fresh |= l.steps == 0;
+        if (fresh && left > 0)
+        {
+            coarse_step(ctx, false, false, 0);
+            left--;
+        }
+        if (left >= 2 && !ctx->graph)
+        {
+            // capture two coarse steps: every level then returns to its parity
+            std::vector<int64_t> saved;
+            for (auto &l : ctx->lv) saved.push_back(l.steps);
+            int64_t saved_done = ctx->coarse_done, saved_launch = ctx->launches;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            coarse_step(ctx, false, false, 0);
+            coarse_step(ctx, false, false, 0);
+            CK(cudaStreamEndCapture(ctx->stream, &g));
+            CK(cudaGraphInstantiate(&ctx->graph, g, 0));
+            CK(cudaGraphDestroy(g));
+            ctx->graph_launches = ctx->launches - saved_launch;
+            for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
+            ctx->coarse_done = saved_done;
+            ctx->launches = saved_launch;
+        }
+        while (left >= 2)
+        {
+            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+            for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps += 2 * ctx->lay.levels[l].substeps;
+            ctx->coarse_done += 2;
+            ctx->launches += ctx->graph_launches;
+            left -= 2;
+        }
+        if (left == 1) coarse_step(ctx, false, false, 0);
+        ctx->ref_t += n_steps;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_step_level(mgpu_ctx *ctx, int level, int n)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || level < 1 || level > (int)ctx->lv.size() || n < 0) throw std::invalid_argument("bad argument");
+        int l = level - 1;
+        const LevelLayout &ll = ctx->lay.levels[l];
+        if (ll.tile_list.empty()) return MGPU_OK;
+        dev::Common C = ctx->common();
+        for (int i = 0; i < n; i++)
+        {
+            dev::StepOpt o{};
+            o.parity = (int)(ctx->lv[l].steps & 1);
+            o.direct = ctx->lv[l].steps == 0 ? 1 : 0;
+            o.snap_use = ctx->grid.multiblock ? 1 : 0;
+            dim3 grid((unsigned)ll.tile_list.size()), block(256);
+            dev::LevelView V = ctx->view(l);
+            if (o.parity == 0) dev::k_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            launch_check(ctx);
+            ctx->lv[l].steps++;
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_level_info(const mgpu_ctx *ctx, int level, int64_t out[4])
+{
+    if (!ctx || !out || level < 1 || level > (int)ctx->lay.levels.size()) return fail(nullptr, MGPU_E_ARG, "bad argument");
+    const LevelLayout &ll = ctx->lay.levels[level - 1];
+    out[0] = ll.n_active;
+    out[1] = ll.n_active_real;
+    out[2] = (int64_t)ll.tile_list.size();
+    out[3] = ll.substeps;
+    return MGPU_OK;
+}
+
+int mgpu_sync(mgpu_ctx *ctx)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx) throw std::invalid_argument("null context");
+        CK(cudaStreamSynchronize(ctx->stream));
+        return MGPU_OK;
+    });
+}
+
+int mgpu_time(const mgpu_ctx *ctx, int64_t *t)
+{
+    if (!ctx || !t) return fail(nullptr, MGPU_E_ARG, "null argument");
+    *t = ctx->ref_t;
+    return MGPU_OK;
+}
+
+int mgpu_residuals(mgpu_ctx *ctx, double *out, int64_t cap, int64_t *count)
+{
+    if (!ctx) return fail(nullptr, MGPU_E_ARG, "null argument");
+    int64_t n = (int64_t)ctx->residuals.size();
+    if (count) *count = n;
+    if (out)
+        for (int64_t i = 0; i < std::min(cap, n); i++) out[i] = ctx->residuals[i];
+    return MGPU_OK;
+}
+
+int mgpu_download_cells(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx) throw std::invalid_argument("null context");
+        int64_t n = ctx->grid.n_cells;
+        int64_t acct = 0;
+        if (ctx->out_rho.n < (size_t)n)
+        {
+            ctx->out_rho.alloc(n, acct);
+            ctx->out_ux.alloc(n, acct);
+            ctx->out_uy.alloc(n, acct);
+        }
+        if (f && ctx->out_f.n < (size_t)n * 9) ctx->out_f.alloc((size_t)n * 9, acct);
+        ctx->bytes += acct;
+        cells_pass(ctx, ctx->out_rho.p, ctx->out_ux.p, ctx->out_uy.p, f ? ctx->out_f.p : nullptr, false, false, -1);
+        if (rho) CK(cudaMemcpyAsync(rho, ctx->out_rho.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (ux) CK(cudaMemcpyAsync(ux, ctx->out_ux.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (uy) CK(cudaMemcpyAsync(uy, ctx->out_uy.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (f) CK(cudaMemcpyAsync(f, ctx->out_f.p, n * 72, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return MGPU_OK;
+    });
+}
+
+int mgpu_download_pixels(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx) throw std::invalid_argument("null context");
+        const Grid &g = ctx->grid;
+        int64_t n = g.n_cells;
+        std::vector<double> r(n), vx(n), vy(n), ff(f ? (size_t)n * 9 : 0);
+        int rc = mgpu_download_cells(ctx, r.data(), vx.data(), vy.data(), f ? ff.data() : nullptr);
+        if (rc) return rc;
+        const size_t nn = (size_t)g.n * g.n;
+        if (rho) std::fill(rho, rho + nn, 0.0);
+        if (ux) std::fill(ux, ux + nn, 0.0);
+        if (uy) std::fill(uy, uy + nn, 0.0);
+        if (f) std::fill(f, f + nn * 9, 0.0);
+        for (int64_t c = 0; c < n; c++)
+        {
+            if (g.is_buffer[c]) continue;
+            int side = 1 << (g.level[c] - 1);
+            for (int yy = g.y[c]; yy < g.y[c] + side; yy++)
+                for (int xx = g.x[c]; xx < g.x[c] + side; xx++)
+                {
+                    size_t p = (size_t)yy * g.n + xx;
+                    if (rho) rho[p] = r[c];
+                    if (ux) ux[p] = vx[c];
+                    if (uy) uy[p] = vy[c];
+                    if (f)
+                        for (int q = 0; q < 9; q++) f[p * 9 + q] = ff[(size_t)c * 9 + q];
+                }
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_observables(mgpu_ctx *ctx, double out[4])
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || !out) throw std::invalid_argument("null argument");
+        const int slot = kRing - 1;
+        zero_slots(ctx, slot, 1);
+        cells_pass(ctx, nullptr, nullptr, nullptr, nullptr, false, false, slot * 4);
+        double v[4];
+        read_slot(ctx, slot, v);
+        CK(cudaStreamSynchronize(ctx->stream));
+        double npix = (double)ctx->grid.n * ctx->grid.n;
+        double mean_ux = v[2] / npix;
+        double nu = (ctx->lay.tau_mean - 0.5) / 3.0;
+        out[0] = mean_ux;
+        out[1] = ctx->prm.fbody != 0 ? mean_ux * nu / ctx->prm.fbody : 0.0;
+        out[2] = v[3];
+        out[3] = ctx->residuals.empty() ? 1.0 : ctx->residuals.back();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_reconstructed(const mgpu_ctx *ctx, int64_t *out)
+{
+    if (!ctx || !out) return fail(nullptr, MGPU_E_ARG, "null argument");
+    std::copy(ctx->grid.reconstructed.begin(), ctx->grid.reconstructed.end(), out);
+    return MGPU_OK;
+}
+
+int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || !rho || !ux || !uy) throw std::invalid_argument("null argument");
+        int64_t n = ctx->grid.n_cells, tmp = 0;
+        DevBuf<double> dr, du, dv;
+        dr.upload(std::vector<double>(rho, rho + n), tmp, ctx->stream);
+        du.upload(std::vector<double>(ux, ux + n), tmp, ctx->stream);
+        dv.upload(std::vector<double>(uy, uy + n), tmp, ctx->stream);
+        for (auto &l : ctx->lv) l.steps = 0;
+        dev::k_set_equilibrium<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, dr.p, du.p, dv.p);
+        launch_check(ctx);
+        CK(cudaStreamSynchronize(ctx->stream));
+        return MGPU_OK;
+    });
+}
+
+int mgpu_set_stream(mgpu_ctx *ctx, void *stream)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx) throw std::invalid_argument("null context");
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (ctx->own_stream) CK(cudaStreamDestroy(ctx->stream));
+        if (ctx->graph)
+        {
+            CK(cudaGraphExecDestroy(ctx->graph));
+            ctx->graph = nullptr;
+        }
+        if (stream)
+        {
+            ctx->stream = (cudaStream_t)stream;
+            ctx->own_stream = false;
+        }
+        else
+        {
+            CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+            ctx->own_stream = true;
+        }
+        return MGPU_OK;
+    });
+}
+
+int64_t mgpu_launch_count(const mgpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+const char *mgpu_last_error(const mgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
+const char *mgpu_global_error(void) { return g_error.c_str(); }
+
+} // extern "C"

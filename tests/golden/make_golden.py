@@ -1,0 +1,161 @@
+"""Generates the golden fixtures under tests/golden/ (run in a checkout that has
+the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
+
+  fixture64.npz     the reference's 64x64 test inputs (test/test_input_output/
+                    {pore,Kn,localporesize}.dat, as row-major images) and its gold
+                    outputs gold/{transport,adsorption}/{ux,uy,rho}.txt (100 steps)
+  refgrid_<case>.npz  grid tables produced by the reference's own Grid2D / LB2D
+                    code (oracle/_ref/ref_driver): the 64x64 test image single-
+                    and multi-block, and block geometries multi-block
+  refstate_<case>.npz per-cell state of the reference's own solver after some
+                    steps for multi-block cases where the reference's
+                    interpolation stays inside its arrays
+
+Usage: python tests/golden/make_golden.py [REF_DIR]
+"""
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
+HOME = ROOT / "oracle" / "_ref" / "home"
+
+
+def read_col_major(path, n):
+    v = np.loadtxt(path)
+    return v.reshape(n, n).T.copy()  # data[j*n + i] belongs to row i, column j
+
+
+def write_col_major(folder, pore, kn, lp):
+    folder.mkdir(parents=True, exist_ok=True)
+    for name, arr, fmt in (("pore.dat", pore, "%d"), ("Kn.dat", kn, "%.6e"), ("localporesize.dat", lp, "%.6e")):
+        np.savetxt(folder / name, arr.T.reshape(-1), fmt=fmt)
+
+
+def read_dump(path):
+    d = path.read_bytes()
+    off = 0
+
+    def take(fmt):
+        nonlocal off
+        v = struct.unpack_from(fmt, d, off)
+        off += struct.calcsize(fmt)
+        return v
+
+    def vec(dt):
+        nonlocal off
+        (k,) = take("q")
+        a = np.frombuffer(d, dtype=dt, count=k, offset=off).copy()
+        off += a.nbytes
+        return a
+
+    return take, vec
+
+
+def read_grid(path):
+    take, vec = read_dump(path)
+    (n,) = take("q")
+    (L,) = take("i")
+    g = dict(n_cells=n, max_level=L)
+    g["ij"] = vec(np.int32).reshape(-1, 2)
+    for k in ("level", "type", "is_buffer", "bnd"):
+        g[k] = vec(np.int32)
+    g["conn"] = vec(np.int64).reshape(-1, 9)
+    for k in ("tau", "kn", "locpore"):
+        g[k] = vec(np.float64)
+    g["lin"] = vec(np.int64)
+    g["stream_id"], g["stream_ic"], g["stream_loc"] = vec(np.int64), vec(np.int32), vec(np.int64)
+    g["wall_id"], g["wall_ic"] = vec(np.int64), vec(np.int32)
+    g["per_id"], g["per_i2"], g["per_ic"] = vec(np.int64), vec(np.int64), vec(np.int32)
+    g["coarse_rows"] = vec(np.int64).reshape(-1, 6)
+    g["fine_rows"] = vec(np.int64).reshape(-1, 6)
+    g["parent_child"] = vec(np.int64).reshape(-1, 5)
+    return g
+
+
+def read_state(path):
+    take, vec = read_dump(path)
+    (step,) = take("q")
+    s = dict(step=step)
+    for k in ("rho", "ux", "uy", "f", "residuals"):
+        s[k] = vec(np.float64)
+    s["f"] = s["f"].reshape(-1, 9)
+    return s
+
+
+def run_ref(folder, n, steps, multiblock, mode="transport", dx=1e-9, levels=2, dump_steps=()):
+    exe = DRIVER if levels == 2 else ROOT / "oracle" / "_ref" / "ref_driver3"
+    with tempfile.TemporaryDirectory() as dump:
+        cmd = [str(exe), "1", "true" if multiblock else "False", str(n), str(folder) + "/", str(steps), "--mode", mode,
+               "--dx", repr(dx), "--quiet", "--no-break", "--dump", dump]
+        if dump_steps:
+            cmd += ["--dump-steps", ",".join(str(s) for s in dump_steps)]
+        env = dict(os.environ, HOME=str(HOME))
+        subprocess.run(cmd, check=True, env=env, stdout=subprocess.DEVNULL)
+        grid = read_grid(Path(dump) / "grid.bin")
+        states = {s: read_state(Path(dump) / f"state_{s}.bin") for s in dump_steps}
+    return grid, states
+
+
+def block_geometry(n, wall, obst=None):
+    p = np.ones((n, n), dtype=np.int32)
+    p[:wall, :] = 0
+    p[n - wall:, :] = 0
+    if obst:
+        r0, r1, c0, c1 = obst
+        p[r0:r1, c0:c1] = 0
+    kn = np.where(p == 1, 0.1, 0.0)
+    lp = np.where(p == 1, 7.73, 0.0)
+    return p, kn, lp
+
+
+CASES = {
+    # name: (n, wall rows, obstacle rows/cols)
+    "channel64": (64, 2, None),
+    "block64": (64, 2, (24, 40, 16, 32)),
+    "block64b": (64, 1, (20, 44, 8, 40)),
+}
+
+
+def main():
+    t = REF / "test" / "test_input_output"
+    fx = dict(
+        pore=read_col_major(t / "pore.dat", 64).astype(np.int32),
+        kn=read_col_major(t / "Kn.dat", 64),
+        locpore=read_col_major(t / "localporesize.dat", 64),
+    )
+    for sim in ("transport", "adsorption"):
+        for name in ("ux", "uy", "rho"):
+            fx[f"{sim}_{name}"] = np.loadtxt(t / "gold" / sim / f"{name}.txt").reshape(64, 64)
+    np.savez_compressed(HERE / "fixture64.npz", **fx)
+
+    with tempfile.TemporaryDirectory() as tmp:
+        # multi-block grid of the 64x64 test image (the reference's interpolation
+        # reads outside its arrays on this image, so only the grid is kept)
+        f = Path(tmp) / "fx64"
+        write_col_major(f, fx["pore"], fx["kn"], fx["locpore"])
+        grid, _ = run_ref(f, 64, 0, True)
+        np.savez_compressed(HERE / "refgrid_fixture64_mb.npz", **grid)
+        grid, _ = run_ref(f, 64, 0, False)
+        np.savez_compressed(HERE / "refgrid_fixture64_sb.npz", **grid)
+        for name, (n, wall, obst) in CASES.items():
+            f = Path(tmp) / name
+            p, kn, lp = block_geometry(n, wall, obst)
+            write_col_major(f, p, kn, lp)
+            grid, states = run_ref(f, n, 50, True, dump_steps=(1, 2, 50))
+            np.savez_compressed(HERE / f"refgrid_{name}.npz", img_pore=p, img_kn=kn, img_locpore=lp, **grid)
+            np.savez_compressed(HERE / f"refstate_{name}.npz",
+                                **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,58 @@
+"""The FP64 CPU oracle is pinned against the reference's golden outputs and
+against the reference's own multi-block code (fixtures made by
+tests/golden/make_golden.py from oracle/_ref)."""
+import numpy as np
+import pytest
+from conftest import load
+
+from mantiis_gb300 import HostGrid, default_params
+from oracle.pyoracle import for_grid
+
+
+def pixels(grid, values, n):
+    out = np.zeros(n * n)
+    out[grid.cells["y"] * n + grid.cells["x"]] = values
+    return out.reshape(n, n)
+
+
+@pytest.mark.parametrize("sim,dx", [("transport", 1e-9), ("adsorption", 12e-9)])
+def test_oracle_reproduces_reference_gold(fixture64, sim, dx):
+    # run_tests.sh: 64x64, single block, 100 steps, max abs difference <= 1e-10
+    g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=dx))
+    o = for_grid(g, sim=sim, dx=dx)
+    assert o.run(100) == 100
+    f = o.fields()
+    for name in ("ux", "uy", "rho"):
+        err = np.abs(pixels(g, f[name], 64) - fixture64[f"{sim}_{name}"]).max()
+        assert err <= 1e-10, (sim, name, err)
+
+
+@pytest.mark.parametrize("case", ["channel64", "block64", "block64b"])
+def test_oracle_multiblock_matches_reference_code(case):
+    ref = load(f"refgrid_{case}.npz")
+    st = load(f"refstate_{case}.npz")
+    g = HostGrid(ref["img_pore"], ref["img_kn"], ref["img_locpore"], default_params(multiblock=1))
+    assert g.max_level == 2
+    o = for_grid(g, sim="transport", dx=1e-9)
+    done = 0
+    for step in (1, 2, 50):
+        o.run(step - done)
+        done = step
+        f = o.fields()
+        for name in ("rho", "ux", "uy"):
+            err = np.abs(f[name] - st[f"{name}_{step}"]).max()
+            assert err <= 1e-12, (case, step, name, err)
+        assert np.abs(f["f"] - st[f"f_{step}"]).max() <= 1e-12
+    assert np.allclose(o.residuals(), st["residuals_50"], rtol=1e-9, atol=0)
+
+
+def test_oracle_break_semantics(fixture64):
+    # the loop stops right after the first step whose residual is below tol
+    g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=1e-9))
+    o = for_grid(g, sim="transport", dx=1e-9)
+    o.run(40)
+    r = o.residuals()
+    tol = float(r[29]) * 1.0000001  # first residual below tol is that of step 30
+    assert (r[:29] > tol).all()
+    o2 = for_grid(g, sim="transport", dx=1e-9, tol=tol)
+    assert o2.run(100, break_on_tol=True) == 30
