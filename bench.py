@@ -96,7 +96,7 @@ def make_images(count, offset):
 def params_for(img):
     from mantiis_gb300 import default_params
 
-    return default_params(multiblock=1, max_allowed_level=3, dx=img["dx"])
+    return default_params(multiblock=1, max_allowed_level=3, dx=img["dx"], edge_fine=1)
 
 
 def cpu_oracle_rate(img, seconds, threads):
@@ -213,6 +213,8 @@ def main():
         ms = float(t.item())
     value = lu_step * world * K / (ms / 1e3) / 1e6
 
+    finite = all(np.isfinite(s.observables()["mean_ux"]) for s in solvers)
+
     # roofline: finest-level step kernel of image 0 on a separate context
     prof = Solver(imgs[0]["pore"], imgs[0]["kn"], imgs[0]["locpore"], params_for(imgs[0]))
     prof.set_stream(stream.cuda_stream)
@@ -270,7 +272,8 @@ def main():
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "images_per_gpu": len(imgs), "n": 1024, "levels": 3,
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
-                       "l2": "inputs larger than L2 (state of the batch > 129 MB)", "graph": "CUDA graph of 2 coarse steps per image"},
+                       "l2": "inputs larger than L2 (state of the batch > 129 MB)",
+                       "graph": "CUDA graph of 2 coarse steps per image", "state_finite_after_timed_steps": finite},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_step level 1", "units_per_launch": lvl1["active"],

@@ -53,6 +53,9 @@ typedef struct mgpu_params
     double rho_noise;      /* half-width of uniform initial density noise (0 = none) */
     uint64_t seed;         /* seed of that noise */
     int check_every;       /* residual evaluated every k coarse steps (1 = every step, as the reference) */
+    int edge_fine;         /* 1: keep the quadtree at the finest level on the x-periodic edges (the
+                              reference's grid, 0, leaves coarse/fine interfaces across that boundary
+                              without buffer cells, which makes the multi-block solution diverge) */
 } mgpu_params;
 
 /* Static description of a built context. */

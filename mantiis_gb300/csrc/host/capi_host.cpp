@@ -56,6 +56,7 @@ GridOptions options_of(const mgpu_params *p)
     o.max_allowed_level = p->max_allowed_level;
     o.dx = p->dx;
     o.mfp = u.mfp;
+    o.edge_fine = p->edge_fine != 0;
     return o;
 }
 } // namespace

@@ -59,6 +59,7 @@ struct Builder
                 if (mn < (double)((size_t)min_dist * (size_t)h)) divide = true;
             }
             if (std::log2((double)h) + 1 > opt.max_allowed_level) divide = true;
+            if (opt.edge_fine && h > 1 && (qc == 0 || qc + h == n)) divide = true;
             if (((1.0 - alpha) < beta && beta < alpha) || divide)
             {
                 decompose(qr, qc, h, min_dist);

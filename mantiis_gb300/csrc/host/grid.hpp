@@ -76,6 +76,12 @@ struct GridOptions
     int max_allowed_level = 2; // quadtree depth limit (include/grid.hpp:1180)
     double dx = 1.0e-9;        // lattice spacing, m (multi-block relaxation times)
     double mfp = 0.0;          // mean free path, m
+    // Keep every quadrant that touches column 0 or column n-1 at the finest
+    // level.  The reference builds no buffer cells across the x-periodic
+    // boundary, so a coarse cell facing finer cells across it loses those
+    // populations every step and the solution diverges; with this option no
+    // coarse/fine interface crosses the boundary.  Off = the reference's grid.
+    bool edge_fine = false;
 };
 
 Grid build_grid(const PoreImage &img, const GridOptions &opt);

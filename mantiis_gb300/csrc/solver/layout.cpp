@@ -196,7 +196,8 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         double r = 0.0;
         if (wall[c])
         {
-            if (p.wall == WALL_SRBB) r = 0.4987 * std::pow(kn, -0.131) - 0.25;
+            if (b < 0) r = 1.0; // wall link of a cell with no boundary type: full bounce-back
+            else if (p.wall == WALL_SRBB) r = 0.4987 * std::pow(kn, -0.131) - 0.25;
             else if (p.wall == WALL_MDBB) r = 0.3222 * std::pow(kn, -0.217) - 0.25;
         }
         rec.r = (float)r;
@@ -313,20 +314,20 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             {
                 int64_t nb = g.conn[(size_t)pc * 9 + q];
                 nb_cell[q] = nb;
-                if (nb < 0)
-                {
-                    // wall / missing neighbour: nominal lattice position, parent's value
-                    X[q] = g.y[pc] + CY[q] * thr + parent_shift + 1;
-                    Y[q] = g.x[pc] + CX[q] * thr + parent_shift + 1;
-                    continue;
-                }
-                int dy = g.y[pc] - g.y[nb], dxv = g.x[pc] - g.x[nb];
+                // neighbour position on the parent's level (periodic), which is
+                // also where a wall / missing neighbour is taken to sit (it then
+                // carries the parent's populations)
+                int ny = ((g.y[pc] + CY[q] * thr) % g.n + g.n) % g.n;
+                int nx = ((g.x[pc] + CX[q] * thr) % g.n + g.n) % g.n;
+                if (nb >= 0 && (g.y[nb] != ny || g.x[nb] != nx))
+                    throw std::runtime_error("layout: neighbour off its lattice position");
+                int dy = g.y[pc] - ny, dxv = g.x[pc] - nx;
                 if (std::abs(dy) > thr && dy < 0) X[q] = g.y[pc] + parent_shift + 1 - 2;
                 else if (std::abs(dy) > thr && dy > 0) X[q] = g.y[pc] + parent_shift + 1 + 2;
-                else X[q] = g.y[nb] + parent_shift + 1;
+                else X[q] = ny + parent_shift + 1;
                 if (std::abs(dxv) > thr && dxv < 0) Y[q] = g.x[pc] + parent_shift + 1 - 2;
                 else if (std::abs(dxv) > thr && dxv > 0) Y[q] = g.x[pc] + parent_shift + 1 + 2;
-                else Y[q] = g.x[nb] + parent_shift + 1;
+                else Y[q] = nx + parent_shift + 1;
             }
             std::vector<double> xs(X, X + 9), ys(Y, Y + 9);
             std::sort(xs.begin(), xs.end());

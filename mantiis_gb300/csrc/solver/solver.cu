@@ -463,6 +463,7 @@ void mgpu_default_params(mgpu_params *p)
     p->rho_noise = 0.0;
     p->seed = 0;
     p->check_every = 1;
+    p->edge_fine = 0;
 }
 
 static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **out)
@@ -487,6 +488,7 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     go.max_allowed_level = p->max_allowed_level;
     go.dx = p->dx;
     go.mfp = ctx->units.mfp;
+    go.edge_fine = p->edge_fine != 0;
     ctx->grid = build_grid(img, go);
     if (ctx->grid.max_level > dev::kMaxLevels) throw std::runtime_error("too many refinement levels");
     transport_only(ctx.get());

@@ -35,6 +35,7 @@ class Params(C.Structure):
         ("rho_noise", C.c_double),
         ("seed", C.c_uint64),
         ("check_every", C.c_int),
+        ("edge_fine", C.c_int),
     ]
 
 

@@ -217,7 +217,7 @@ struct Oracle
         {
             int64_t c = boundaryID[i];
             if (level[c] != lvl) continue;
-            double r = 0.4987 * std::pow(kn[c], -0.131) - 0.25;
+            double r = bnd[c] < 0 ? 1.0 : 0.4987 * std::pow(kn[c], -0.131) - 0.25;
             int q = boundaryIC[i];
             f[c * NC + OPPO[q]] += r * ftemp[c * NC + q];
             f[c * NC + icsr_of(c, q)] += (1 - r) * ftemp[c * NC + q];
@@ -239,7 +239,7 @@ struct Oracle
                 if (cn > 0) kdeno += feq[k1 * NC + ic];
                 else if (cn < 0) kno += fb[k1 * NC + ic];
             }
-            double r = 0.3222 * std::pow(kn[k1], -0.217) - 0.25;
+            double r = bnd[k1] < 0 ? 1.0 : 0.3222 * std::pow(kn[k1], -0.217) - 0.25;
             f[k1 * NC + OPPO[k2]] = r * ftemp[k1 * NC + k2] + (1 - r) * kno / kdeno * feq[k1 * NC + OPPO[k2]];
         }
     }
@@ -415,8 +415,9 @@ struct Oracle
 
     // include/coreLB.hpp:1101-1231, with defined meanings where the reference
     // reads outside its arrays: a missing coarse child is left out of the mean;
-    // a wall/missing neighbour of a fine-buffer parent takes the nominal lattice
-    // position and the parent's own populations.
+    // a wall/missing neighbour of a fine-buffer parent takes its periodic
+    // lattice position and the parent's own populations.  A wall link of a cell
+    // without boundary type (reference: ifStream[-1]) is a full bounce-back.
     void interpolate(int l1, int l2)
     {
         int key = l2 * 10 + l1;
@@ -457,18 +458,15 @@ struct Oracle
             {
                 int64_t nb = conn[pc * 9 + ic];
                 pconn[ic] = nb >= 0 ? nb : pc;
-                if (nb < 0)
-                {
-                    X[ic] = y[pc] + EY[ic] * thr + parent_shift + 1;
-                    Y[ic] = x[pc] + EX[ic] * thr + parent_shift + 1;
-                    continue;
-                }
-                if (std::abs(y[pc] - y[nb]) > thr && y[pc] - y[nb] < 0) X[ic] = y[pc] + parent_shift + 1 - 2;
-                else if (std::abs(y[pc] - y[nb]) > thr && y[pc] - y[nb] > 0) X[ic] = y[pc] + parent_shift + 1 + 2;
-                else X[ic] = y[nb] + parent_shift + 1;
-                if (std::abs(x[pc] - x[nb]) > thr && x[pc] - x[nb] < 0) Y[ic] = x[pc] + parent_shift + 1 - 2;
-                else if (std::abs(x[pc] - x[nb]) > thr && x[pc] - x[nb] > 0) Y[ic] = x[pc] + parent_shift + 1 + 2;
-                else Y[ic] = x[nb] + parent_shift + 1;
+                // a wall / missing neighbour sits at its periodic lattice position
+                int yn = nb >= 0 ? y[nb] : (int)(((y[pc] + EY[ic] * (int)thr) % n + n) % n);
+                int xn = nb >= 0 ? x[nb] : (int)(((x[pc] + EX[ic] * (int)thr) % n + n) % n);
+                if (std::abs(y[pc] - yn) > thr && y[pc] - yn < 0) X[ic] = y[pc] + parent_shift + 1 - 2;
+                else if (std::abs(y[pc] - yn) > thr && y[pc] - yn > 0) X[ic] = y[pc] + parent_shift + 1 + 2;
+                else X[ic] = yn + parent_shift + 1;
+                if (std::abs(x[pc] - xn) > thr && x[pc] - xn < 0) Y[ic] = x[pc] + parent_shift + 1 - 2;
+                else if (std::abs(x[pc] - xn) > thr && x[pc] - xn > 0) Y[ic] = x[pc] + parent_shift + 1 + 2;
+                else Y[ic] = xn + parent_shift + 1;
             }
             std::vector<double> Xs(X, X + 9), Ys(Y, Y + 9);
             std::sort(Xs.begin(), Xs.end());
