@@ -87,16 +87,26 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def make_images(count, offset):
+WORKLOADS = {
+    "config2": WORKLOAD,
+    "single1024": "1024x1024 seeded disk images (r U[6,40], porosity 0.6), single block, Kn 0.1",
+}
+
+
+def make_images(count, offset, workload="config2"):
     from mantiis_gb300 import workloads
 
-    return [workloads.config2(offset + i) for i in range(count)]
+    if workload == "single1024":
+        return [dict(workloads.image(1024, 6, 40, 0.6, 0.1, 5000 + offset + i), levels=1) for i in range(count)]
+    return [dict(workloads.config2(offset + i), levels=3) for i in range(count)]
 
 
 def params_for(img):
     from mantiis_gb300 import default_params
 
-    return default_params(multiblock=1, max_allowed_level=3, dx=img["dx"], edge_fine=1)
+    if img.get("levels", 3) == 1:
+        return default_params(multiblock=0, dx=img["dx"])
+    return default_params(multiblock=1, max_allowed_level=img["levels"], dx=img["dx"], edge_fine=1)
 
 
 def cpu_oracle_rate(img, seconds, threads):
@@ -156,6 +166,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -176,8 +187,12 @@ def main():
         dist.init_process_group("nccl")
     from mantiis_gb300 import Solver
 
-    imgs = make_images(args.images, rank * args.images)
-    stream = torch.cuda.current_stream()
+    imgs = make_images(args.images, rank * args.images, args.workload)
+    # a dedicated (non-default) stream: every context enqueues on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     solvers = []
     for img in imgs:
         s = Solver(img["pore"], img["kn"], img["locpore"], params_for(img))
@@ -235,7 +250,7 @@ def main():
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get("k_step_level1_bytes_per_launch")
+            traffic = json.loads(tfile.read_text()).get("level1_substep_bytes")
         except Exception:
             traffic = None
     prof.close()
@@ -270,13 +285,14 @@ def main():
             "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": warm,
             "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "images_per_gpu": len(imgs), "n": 1024, "levels": 3,
+            "config": {"workload": WORKLOADS[args.workload], "images_per_gpu": len(imgs), "n": 1024,
+                       "levels": imgs[0]["levels"],
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
                        "l2": "inputs larger than L2 (state of the batch > 129 MB)",
                        "graph": "CUDA graph of 2 coarse steps per image", "state_finite_after_timed_steps": finite},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_step level 1", "units_per_launch": lvl1["active"],
+                         "kernel": "level-1 substep (k_plain + k_special)", "units_per_launch": lvl1["active"],
                          "bytes_per_unit": BYTES_PER_LU, "ms_per_launch": k_ms},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,

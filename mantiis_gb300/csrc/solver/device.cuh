@@ -256,6 +256,27 @@ template <int P> __device__ __forceinline__ void load_raw(const LevelView &L, in
     }
 }
 
+// same reads through the read-only data path (the slots read by a thread are
+// written only by that thread in the same launch)
+template <int P> __device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, float raw[9])
+{
+    if (P == 0)
+    {
+        const int64_t s = site_of(L, x, y);
+#pragma unroll
+        for (int q = 0; q < 9; q++) raw[q] = __ldg(&L.f[q * L.plane + s]);
+    }
+    else
+    {
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+        {
+            const int xs = wrapx(x - d2q9::cx(q), L.W), ys = wrapx(y - d2q9::cy(q), L.H);
+            raw[q] = __ldg(&L.f[d2q9::opp(q) * L.plane + site_of(L, xs, ys)]);
+        }
+    }
+}
+
 template <int P> __device__ __forceinline__ void store_post(const LevelView &L, int x, int y, const float fs[9])
 {
     if (P == 0)

@@ -83,100 +83,142 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
     return -tau;
 }
 
-// One lattice update of every active site of one level (transport step body:
-// equilibrium, regularized MRT / MRT / BGK collision, streaming, walls,
-// x-periodicity; include/coreLB.hpp:420-430, 646-792, 834-977, 1018-1054).
-// One thread per site, 32x8 sites per block, blocks over the active tiles.
-template <int P> __global__ void __launch_bounds__(256) k_step(LevelView L, Common C, StepOpt o)
+// Collision and streaming of one cell whose populations df are loaded:
+// macroscopic moments (and the residual / snapshot side outputs), equilibrium,
+// regularized MRT / MRT / BGK collision, the wall values of special cells and
+// the AA-pattern store (include/coreLB.hpp:420-430, 646-792, 834-977, 1018-1054).
+template <int P>
+__device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y, int64_t s,
+                                          const float df[9], float tau_s, bool special, const SpecialRec &rec,
+                                          double &r_diff, double &r_norm)
 {
-    const int tile = L.tiles[blockIdx.x];
+    float drho, rho, ux, uy;
+    macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
+    if (o.diff | o.store_u)
+    {
+        const float un = sqrtf(ux * ux + uy * uy);
+        if (o.diff)
+        {
+            r_diff = (double)fabsf(un - L.unorm[s]);
+            r_norm = (double)un;
+        }
+        if (o.store_u) L.unorm[s] = un;
+    }
+    if (o.snap_store)
+    {
+        L.snap[s] = drho;
+        L.snap[L.plane + s] = ux;
+        L.snap[2 * L.plane + s] = uy;
+    }
+    float edrho = drho, erho = rho, eux = ux, euy = uy;
+    if (o.snap_use)
+    {
+        edrho = L.snap[s];
+        erho = C.rho0 + edrho;
+        eux = L.snap[L.plane + s];
+        euy = L.snap[2 * L.plane + s];
+    }
+    float feq[9], fs[9];
+    equilibrium(edrho, erho, eux, euy, feq);
+    if (C.collision == COLL_RMRT) collide_rmrt(df, feq, tau_s, fs);
+    else if (C.collision == COLL_MRT) collide_mrt(df, feq, tau_s, L.tau2 ? L.tau2[s] : 1.0f, fs);
+    else
+    {
+        const float inv_tau = 1.0f; // 1 / tau_SRT, tau_SRT = 1 (include/globalParameters.hpp:140)
+#pragma unroll
+        for (int q = 0; q < 9; q++) fs[q] = df[q] - inv_tau * (df[q] - feq[q]);
+    }
+    if (special)
+    {
+        const uint32_t wall = (rec.m0 >> 18) & 0x1FFu, quirk = rec.m1 & 0x1FFu;
+        if (wall && C.wall == WALL_MDBB)
+        {
+            // include/coreLB.hpp:936-967: reflected value
+            //   r f*_q + (1 - r) (sum_{c.n<0} f / sum_{c.n>0} f_eq) f_eq,opp(q)
+            // in deviation form; both sums share the weight total A.
+            const uint32_t bnd = (rec.m1 >> 9) & 0xFFu;
+            const uint32_t pos = bnd == 0xFFu ? 0u : c_npos[bnd], neg = bnd == 0xFFu ? 0u : c_nneg[bnd];
+            float a = 0.f, ap = 0.f, A = 0.f;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+            {
+                if ((neg >> q) & 1u) a += df[q];
+                if ((pos >> q) & 1u)
+                {
+                    ap += feq[q];
+                    A += wq(q) * C.rho0;
+                }
+            }
+            const float g = (A + ap) != 0.f ? (a - ap) / (A + ap) : 0.f;
+            const float r = rec.r;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+                if ((wall >> q) & 1u)
+                {
+                    const int po = d2q9::opp(q);
+                    fs[q] = r * fs[q] + (1.0f - r) * (feq[po] + (wq(po) * C.rho0 + feq[po]) * g);
+                }
+        }
+        if (quirk)
+        {
+            float *side_now = C.side + (size_t)P * C.n_quirk;
+            int qi = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+                if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
+        }
+    }
+    store_post<P>(L, x, y, fs);
+}
+
+// Plain cells of one level (all nine populations stream in, no wall link):
+// one thread per site, 32x8 sites per block, blocks over the active tiles.
+// Each slot a thread reads is written by that thread alone in this launch (AA
+// ownership), so the loads take the read-only path.
+template <int P> __global__ void __launch_bounds__(256, 6) k_plain(LevelView L, Common C, StepOpt o)
+{
+    const int tile = __ldg(&L.tiles[blockIdx.x]);
     const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
     const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
     double r_diff = 0.0, r_norm = 0.0;
-    if (x < L.W && y < L.H && L.tau[site_of(L, x, y)] != 0.0f)
+    if (x < L.W && y < L.H)
     {
         const int64_t s = site_of(L, x, y);
+        const float tau = __ldg(&L.tau[s]);
+        if (tau > 0.0f)
+        {
+            float df[9];
+            if (o.direct) load_raw_ro<0>(L, x, y, df);
+            else load_raw_ro<P>(L, x, y, df);
+            SpecialRec none;
+            step_cell<P>(L, C, o, x, y, s, df, tau, false, none, r_diff, r_norm);
+        }
+    }
+    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+}
+
+// Special cells of one level, from the level's site-sorted record range.
+template <int P>
+__global__ void __launch_bounds__(128) k_special(LevelView L, Common C, StepOpt o, int64_t begin, int count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double r_diff = 0.0, r_norm = 0.0;
+    if (i < count)
+    {
+        const SpecialRec rec = C.specials[begin + i];
+        const int x = rec.site % L.pitch, y = rec.site / L.pitch;
         float df[9];
-        bool special;
-        SpecialRec rec;
-        const float tau_s = load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
-        float drho, rho, ux, uy;
-        macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
-        if (o.diff | o.store_u)
+        const uint32_t flags = rec.m1 >> 17;
+        if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
         {
-            const float un = sqrtf(ux * ux + uy * uy);
-            if (o.diff)
-            {
-                r_diff = (double)fabsf(un - L.unorm[s]);
-                r_norm = (double)un;
-            }
-            if (o.store_u) L.unorm[s] = un;
+#pragma unroll
+            for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + rec.buf];
         }
-        if (o.snap_store)
-        {
-            L.snap[s] = drho;
-            L.snap[L.plane + s] = ux;
-            L.snap[2 * L.plane + s] = uy;
-        }
-        float edrho = drho, erho = rho, eux = ux, euy = uy;
-        if (o.snap_use)
-        {
-            edrho = L.snap[s];
-            erho = C.rho0 + edrho;
-            eux = L.snap[L.plane + s];
-            euy = L.snap[2 * L.plane + s];
-        }
-        float feq[9], fs[9];
-        equilibrium(edrho, erho, eux, euy, feq);
-        if (C.collision == COLL_RMRT) collide_rmrt(df, feq, tau_s, fs);
-        else if (C.collision == COLL_MRT) collide_mrt(df, feq, tau_s, L.tau2 ? L.tau2[s] : 1.0f, fs);
+        else if (o.direct)
+            load_raw<0>(L, x, y, df);
         else
-        {
-            const float inv_tau = 1.0f; // 1 / tau_SRT, tau_SRT = 1 (include/globalParameters.hpp:140)
-#pragma unroll
-            for (int q = 0; q < 9; q++) fs[q] = df[q] - inv_tau * (df[q] - feq[q]);
-        }
-        if (special)
-        {
-            const uint32_t wall = (rec.m0 >> 18) & 0x1FFu, quirk = rec.m1 & 0x1FFu;
-            if (wall && C.wall == WALL_MDBB)
-            {
-                // include/coreLB.hpp:936-967: reflected value
-                //   r f*_q + (1 - r) (sum_{c.n<0} f / sum_{c.n>0} f_eq) f_eq,opp(q)
-                // in deviation form; both sums share the weight total A.
-                const uint32_t bnd = (rec.m1 >> 9) & 0xFFu;
-                const uint32_t pos = bnd == 0xFFu ? 0u : c_npos[bnd], neg = bnd == 0xFFu ? 0u : c_nneg[bnd];
-                float a = 0.f, ap = 0.f, A = 0.f;
-#pragma unroll
-                for (int q = 0; q < 9; q++)
-                {
-                    if ((neg >> q) & 1u) a += df[q];
-                    if ((pos >> q) & 1u)
-                    {
-                        ap += feq[q];
-                        A += wq(q) * C.rho0;
-                    }
-                }
-                const float g = (A + ap) != 0.f ? (a - ap) / (A + ap) : 0.f;
-                const float r = rec.r;
-#pragma unroll
-                for (int q = 0; q < 9; q++)
-                    if ((wall >> q) & 1u)
-                    {
-                        const int po = d2q9::opp(q);
-                        fs[q] = r * fs[q] + (1.0f - r) * (feq[po] + (wq(po) * C.rho0 + feq[po]) * g);
-                    }
-            }
-            if (quirk)
-            {
-                float *side_now = C.side + (size_t)P * C.n_quirk;
-                int qi = 0;
-#pragma unroll
-                for (int q = 0; q < 9; q++)
-                    if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
-            }
-        }
-        store_post<P>(L, x, y, fs);
+            load_special<P>(L, C, rec, x, y, df);
+        step_cell<P>(L, C, o, x, y, (int64_t)rec.site, df, rec.tau, true, rec, r_diff, r_norm);
     }
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }

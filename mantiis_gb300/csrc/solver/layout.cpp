@@ -168,6 +168,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             if (row[k] >= 0 && g.is_buffer[row[k]]) want_buf(row[k]);
 
     const uint32_t ALL = 0x1FFu;
+    std::vector<int> spec_level;
     for (int64_t c = 0; c < N; c++)
     {
         int l = g.level[c];
@@ -239,9 +240,33 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             for (int q = 0; q < 9; q++) L.ktab.push_back((float)(p.rho0 * K[q]));
             rec.m1 |= (uint32_t)SF_HAS_K << 17;
         }
+        rec.site = s;
+        rec.tau = tau;
         lv.tau[(size_t)s] = -tau;
-        lv.spec[(size_t)s] = (uint32_t)L.specials.size();
         L.specials.push_back(rec);
+        spec_level.push_back(l);
+    }
+    // special records grouped by level and sorted by site, so the special-cell
+    // kernel of a level walks a contiguous, spatially ordered range
+    {
+        std::vector<int64_t> order(L.specials.size());
+        for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
+        std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+            if (spec_level[a] != spec_level[b]) return spec_level[a] < spec_level[b];
+            return L.specials[a].site < L.specials[b].site;
+        });
+        std::vector<SpecialRec> sorted(order.size());
+        for (size_t i = 0; i < order.size(); i++) sorted[i] = L.specials[order[i]];
+        L.specials.swap(sorted);
+        for (auto &lv : L.levels) lv.spec_count = 0;
+        for (size_t i = 0; i < L.specials.size(); i++)
+        {
+            int l = spec_level[order[i]];
+            LevelLayout &lv = L.levels[l - 1];
+            if (lv.spec_count == 0) lv.spec_begin = (int64_t)i;
+            lv.spec_count++;
+            lv.spec[(size_t)L.specials[i].site] = (uint32_t)i;
+        }
     }
 
     // active tiles (32 x 8 sites)

@@ -55,7 +55,8 @@ struct alignas(16) SpecialRec
     int32_t quirk_base;// side-buffer slot of this cell's first quirk link
     int32_t k_row;     // row of the constant-term table (SF_HAS_K)
     int32_t buf;       // interpolation buffer index (SF_BUFFER), else -1
-    float pad0 = 0.f, pad1 = 0.f;
+    int32_t site;      // site of the cell on its level
+    float tau;         // tau_s of the cell
 };
 
 struct LevelLayout
@@ -70,6 +71,7 @@ struct LevelLayout
     int tiles_x = 0, tiles_y = 0;
     int64_t n_active = 0, n_active_real = 0;
     int substeps = 1;                // per coarse step, 2^(L-l)
+    int64_t spec_begin = 0, spec_count = 0; // this level's special records (sorted by site)
     bool snapshot_all = false;       // level keeps the coarse-step-start (rho,u) of all cells
 };
 

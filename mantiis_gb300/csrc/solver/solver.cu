@@ -280,6 +280,28 @@ void launch_check(mgpu_ctx *ctx)
     CK(cudaGetLastError());
 }
 
+// the two kernels of one substep of one level: plain cells over the active
+// tiles, special cells over the level's record range (disjoint slot sets)
+void launch_level(mgpu_ctx *ctx, int l, const dev::LevelView &V, const dev::Common &C, const dev::StepOpt &o)
+{
+    const LevelLayout &ll = ctx->lay.levels[l];
+    if (!ll.tile_list.empty())
+    {
+        dim3 grid((unsigned)ll.tile_list.size()), block(256);
+        if (o.parity == 0) dev::k_plain<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+        else dev::k_plain<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+        launch_check(ctx);
+    }
+    if (ll.spec_count)
+    {
+        int n = (int)ll.spec_count;
+        dim3 grid((unsigned)((n + 127) / 128)), block(128);
+        if (o.parity == 0) dev::k_special<0><<<grid, block, 0, ctx->stream>>>(V, C, o, ll.spec_begin, n);
+        else dev::k_special<1><<<grid, block, 0, ctx->stream>>>(V, C, o, ll.spec_begin, n);
+        launch_check(ctx);
+    }
+}
+
 // ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
 void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
 {
@@ -306,10 +328,7 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
             o.diff = (sub == 0 && diff) ? 1 : 0;
             o.store_u = (sub == 0 && store_u) ? 1 : 0;
             o.red_slot = red_slot;
-            dim3 grid((unsigned)ll.tile_list.size()), block(256);
-            if (o.parity == 0) dev::k_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            launch_check(ctx);
+            launch_level(ctx, l, V, C, o);
             ctx->lv[l].steps++;
         }
     }
@@ -772,11 +791,8 @@ int mgpu_step_level(mgpu_ctx *ctx, int level, int n)
             o.parity = (int)(ctx->lv[l].steps & 1);
             o.direct = ctx->lv[l].steps == 0 ? 1 : 0;
             o.snap_use = ctx->grid.multiblock ? 1 : 0;
-            dim3 grid((unsigned)ll.tile_list.size()), block(256);
             dev::LevelView V = ctx->view(l);
-            if (o.parity == 0) dev::k_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            launch_check(ctx);
+            launch_level(ctx, l, V, C, o);
             ctx->lv[l].steps++;
         }
         return MGPU_OK;
