@@ -28,7 +28,7 @@ __constant__ unsigned short c_nneg[MANTIIS_N_BND_TYPES];
 struct LevelView
 {
     float *f;             // 9 * plane
-    const float *tau;     // per site: 0 inactive, >0 plain, <0 special
+    const float *omega;   // per site 1/tau_s: 0 inactive, >0 plain, <0 special
     const uint32_t *spec; // per site special index
     const float *tau2;    // per site second relaxation time (plain MRT: tau_d), may be null
     float *snap;          // 3 * plane: coarse-step-start (drho, ux, uy), may be null
@@ -36,6 +36,7 @@ struct LevelView
     float *psi;           // per site pseudopotential (adsorption), may be null
     float *force;         // 2 * plane: (Fx, Fy) of the current step (adsorption), may be null
     const int32_t *tiles; // active 32x8 tiles
+    const uint32_t *tile_mask; // 8 row masks of plain cells per active tile
     int ntiles, tiles_x;
     int W, H, pitch;
     int64_t plane;
@@ -112,43 +113,44 @@ __device__ __forceinline__ void equilibrium(float drho, float rho, float ux, flo
 }
 
 // Regularized MRT (include/coreLB.hpp:646-675, 744-792): the non-equilibrium
-// part is projected on its second-order Hermite content Pi, then relaxed in
-// moment space with diag(1, 1/1.1, 1/1.2, 1, 1/tau_q, 1, 1/tau_q, 1/tau_s, 1/tau_s).
-// Only e, epsilon, p_xx, p_xy of the projection are non-zero:
-//   e = 3 T, epsilon = -3 T, p_xx = Pxx - Pyy, p_xy = Pxy  (T = Pxx + Pyy)
-// and M^-1 applied to the relaxed moments gives the closed form below.
-__device__ __forceinline__ void collide_rmrt(const float df[9], const float feq[9], float tau_s, float out[9])
+// part f - f_eq is projected on its second-order Hermite content
+// Pi = sum c c (f - f_eq), then relaxed in moment space with
+// diag(1, 1/1.1, 1/1.2, 1, 1/tau_q, 1, 1/tau_q, 1/tau_s, 1/tau_s).  The
+// projection has only e = 3T, epsilon = -3T, p_xx = N, p_xy = Pxy non-zero
+// (T = Pxx + Pyy, N = Pxx - Pyy), so M^-1 applied to the relaxed moments
+// reduces to
+//   f* = f_eq + k0 T                      (rest)
+//   f* = f_eq + ka T +- (1 - omega) N / 4   (axes x / y)
+//   f* = f_eq + kd T +- (1 - omega) Pxy / 4 (diagonals +- c_x c_y)
+// with k0 = -2/3 + (3/1.1 + 2.5)/9, ka = 1/12 + 3/39.6 - 2.5/18,
+// kd = 1/12 - 3/19.8 + 2.5/36 (the bulk moments relax at 1/1.1 and 1/1.2).
+// Pi comes from the moments of f minus those of f_eq, rho (cs^2 I + u u).
+__device__ __forceinline__ void collide_rmrt(const float df[9], const float feq[9], float drho_e, float rho_e, float ux,
+                                             float uy, float omega, float out[9])
 {
-    float fn[9];
-#pragma unroll
-    for (int q = 0; q < 9; q++) fn[q] = df[q] - feq[q];
-    const float Pxx = fn[1] + fn[3] + fn[5] + fn[6] + fn[7] + fn[8];
-    const float Pyy = fn[2] + fn[4] + fn[5] + fn[6] + fn[7] + fn[8];
-    const float Pxy = fn[5] - fn[6] + fn[7] - fn[8];
-    const float T = Pxx + Pyy;
-    // regularized non-equilibrium: w_q * 4.5 * [(cx^2 - 1/3) Pxx + 2 cx cy Pxy + (cy^2 - 1/3) Pyy]
-    const float r0 = kW0 * 4.5f * (-T * (1.0f / 3.0f));
-    const float rx = kW1 * 4.5f * ((2.0f / 3.0f) * Pxx - (1.0f / 3.0f) * Pyy);
-    const float ry = kW1 * 4.5f * ((2.0f / 3.0f) * Pyy - (1.0f / 3.0f) * Pxx);
-    const float rdp = kW2 * 4.5f * ((2.0f / 3.0f) * T + 2.0f * Pxy);
-    const float rdm = kW2 * 4.5f * ((2.0f / 3.0f) * T - 2.0f * Pxy);
-    const float inv_ts = 1.0f / tau_s;
-    const float a = 3.0f * T * (1.0f / 1.1f);
-    const float b = -3.0f * T * (1.0f / 1.2f);
-    const float c = (Pxx - Pyy) * inv_ts;
-    const float d = Pxy * inv_ts;
-    const float d0 = (-a + b) * (1.0f / 9.0f);
-    const float dax = -a * (1.0f / 36.0f) - b * (1.0f / 18.0f);
-    const float ddg = a * (1.0f / 18.0f) + b * (1.0f / 36.0f);
-    out[0] = feq[0] + r0 - d0;
-    out[1] = feq[1] + rx - (dax + 0.25f * c);
-    out[3] = feq[3] + rx - (dax + 0.25f * c);
-    out[2] = feq[2] + ry - (dax - 0.25f * c);
-    out[4] = feq[4] + ry - (dax - 0.25f * c);
-    out[5] = feq[5] + rdp - (ddg + 0.25f * d);
-    out[7] = feq[7] + rdp - (ddg + 0.25f * d);
-    out[6] = feq[6] + rdm - (ddg - 0.25f * d);
-    out[8] = feq[8] + rdm - (ddg - 0.25f * d);
+    constexpr float k0 = (float)(-2.0 / 3.0 + (3.0 / 1.1 + 2.5) / 9.0);
+    constexpr float ka = (float)(1.0 / 12.0 + 3.0 / 39.6 - 2.5 / 18.0);
+    constexpr float kd = (float)(1.0 / 12.0 - 3.0 / 19.8 + 2.5 / 36.0);
+    const float sd = (df[5] + df[6]) + (df[7] + df[8]);
+    const float sxx = (df[1] + df[3]) + sd;
+    const float syy = (df[2] + df[4]) + sd;
+    const float sxy = (df[5] - df[6]) + (df[7] - df[8]);
+    const float d3 = drho_e * (1.0f / 3.0f);
+    const float Pxx = sxx - (d3 + rho_e * ux * ux);
+    const float Pyy = syy - (d3 + rho_e * uy * uy);
+    const float Pxy = sxy - rho_e * ux * uy;
+    const float T = Pxx + Pyy, N = Pxx - Pyy;
+    const float g = 0.25f * (1.0f - omega);
+    const float at = ka * T, gn = g * N, dt = kd * T, gp = g * Pxy;
+    out[0] = feq[0] + k0 * T;
+    out[1] = feq[1] + (at + gn);
+    out[3] = feq[3] + (at + gn);
+    out[2] = feq[2] + (at - gn);
+    out[4] = feq[4] + (at - gn);
+    out[5] = feq[5] + (dt + gp);
+    out[7] = feq[7] + (dt + gp);
+    out[6] = feq[6] + (dt - gp);
+    out[8] = feq[8] + (dt - gp);
 }
 
 // Moment matrix M and its inverse (include/globalParameters.hpp:154-175).
@@ -258,13 +260,22 @@ template <int P> __device__ __forceinline__ void load_raw(const LevelView &L, in
 
 // same reads through the read-only data path (the slots read by a thread are
 // written only by that thread in the same launch)
-template <int P> __device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, float raw[9])
+template <int P>
+__device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, float raw[9], bool interior = false)
 {
     if (P == 0)
     {
         const int64_t s = site_of(L, x, y);
 #pragma unroll
         for (int q = 0; q < 9; q++) raw[q] = __ldg(&L.f[q * L.plane + s]);
+    }
+    else if (interior)
+    {
+        // no neighbour wraps around the torus: plain offsets
+        const int64_t s = site_of(L, x, y);
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            raw[q] = __ldg(&L.f[d2q9::opp(q) * L.plane + s - d2q9::cy(q) * (int64_t)L.pitch - d2q9::cx(q)]);
     }
     else
     {
@@ -277,13 +288,20 @@ template <int P> __device__ __forceinline__ void load_raw_ro(const LevelView &L,
     }
 }
 
-template <int P> __device__ __forceinline__ void store_post(const LevelView &L, int x, int y, const float fs[9])
+template <int P>
+__device__ __forceinline__ void store_post(const LevelView &L, int x, int y, const float fs[9], bool interior = false)
 {
     if (P == 0)
     {
         const int64_t s = site_of(L, x, y);
 #pragma unroll
         for (int q = 0; q < 9; q++) L.f[d2q9::opp(q) * L.plane + s] = fs[q];
+    }
+    else if (interior)
+    {
+        const int64_t s = site_of(L, x, y);
+#pragma unroll
+        for (int q = 0; q < 9; q++) L.f[q * L.plane + s + d2q9::cy(q) * (int64_t)L.pitch + d2q9::cx(q)] = fs[q];
     }
     else
     {

@@ -55,19 +55,19 @@ __device__ __forceinline__ void block_add2(double a, double b, double *dst)
 }
 
 // Loads the populations of a cell of level view L for a step (or a read) at
-// parity P.  Returns |tau_s| and, for special cells, a copy of the record.
+// parity P.  Returns 1/tau_s and, for special cells, a copy of the record.
 template <int P>
 __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, int x, int y, int direct, int first_sub,
                                            float df[9], bool &special, SpecialRec &rec)
 {
     const int64_t s = site_of(L, x, y);
-    float tau = L.tau[s];
-    special = tau < 0.0f;
+    float om = L.omega[s];
+    special = om < 0.0f;
     if (!special)
     {
         if (direct) load_raw<0>(L, x, y, df);
         else load_raw<P>(L, x, y, df);
-        return tau;
+        return om;
     }
     rec = C.specials[L.spec[s]];
     const uint32_t flags = rec.m1 >> 17;
@@ -80,7 +80,7 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
         load_raw<0>(L, x, y, df);
     else
         load_special<P>(L, C, rec, x, y, df);
-    return -tau;
+    return -om;
 }
 
 // Collision and streaming of one cell whose populations df are loaded:
@@ -89,8 +89,8 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
 // the AA-pattern store (include/coreLB.hpp:420-430, 646-792, 834-977, 1018-1054).
 template <int P>
 __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y, int64_t s,
-                                          const float df[9], float tau_s, bool special, const SpecialRec &rec,
-                                          double &r_diff, double &r_norm)
+                                          const float df[9], float omega, bool special, const SpecialRec &rec,
+                                          double &r_diff, double &r_norm, bool interior = false)
 {
     float drho, rho, ux, uy;
     macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
@@ -120,8 +120,8 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
     }
     float feq[9], fs[9];
     equilibrium(edrho, erho, eux, euy, feq);
-    if (C.collision == COLL_RMRT) collide_rmrt(df, feq, tau_s, fs);
-    else if (C.collision == COLL_MRT) collide_mrt(df, feq, tau_s, L.tau2 ? L.tau2[s] : 1.0f, fs);
+    if (C.collision == COLL_RMRT) collide_rmrt(df, feq, edrho, erho, eux, euy, omega, fs);
+    else if (C.collision == COLL_MRT) collide_mrt(df, feq, 1.0f / omega, L.tau2 ? L.tau2[s] : 1.0f, fs);
     else
     {
         const float inv_tau = 1.0f; // 1 / tau_SRT, tau_SRT = 1 (include/globalParameters.hpp:140)
@@ -168,7 +168,7 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
                 if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
         }
     }
-    store_post<P>(L, x, y, fs);
+    store_post<P>(L, x, y, fs, interior);
 }
 
 // Plain cells of one level (all nine populations stream in, no wall link):
@@ -177,22 +177,77 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
 // ownership), so the loads take the read-only path.
 template <int P> __global__ void __launch_bounds__(256, 6) k_plain(LevelView L, Common C, StepOpt o)
 {
+    // the tile id and this row's plain-cell mask are independent loads, so the
+    // relaxation rate and the populations are then fetched together
     const int tile = __ldg(&L.tiles[blockIdx.x]);
-    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
-    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    const uint32_t mask = __ldg(&L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)]);
+    const int tx = tile % L.tiles_x, ty = tile / L.tiles_x;
+    const int x = tx * 32 + (threadIdx.x & 31);
+    const int y = ty * 8 + (threadIdx.x >> 5);
+    // tiles off the border reach their neighbours without wrapping
+    const bool interior = tx > 0 && tx + 1 < L.tiles_x && ty > 0 && ty + 1 < (L.H + 7) / 8;
     double r_diff = 0.0, r_norm = 0.0;
-    if (x < L.W && y < L.H)
+    if ((mask >> (threadIdx.x & 31)) & 1u)
     {
         const int64_t s = site_of(L, x, y);
-        const float tau = __ldg(&L.tau[s]);
-        if (tau > 0.0f)
+        float df[9];
+        if (o.direct) load_raw_ro<0>(L, x, y, df);
+        else load_raw_ro<P>(L, x, y, df, interior);
+        const float om = __ldg(&L.omega[s]);
+        SpecialRec none;
+        step_cell<P>(L, C, o, x, y, s, df, om, false, none, r_diff, r_norm, interior);
+    }
+    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+}
+
+// Persistent, software-pipelined variant of k_plain: each block walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ... and issues the loads of its
+// next tile before colliding and storing the current one, so that memory
+// requests stay in flight during the arithmetic.  The next tile's slots are
+// disjoint from the current tile's (AA ownership), so the early loads are safe.
+template <int P> __global__ void __launch_bounds__(256, 4) k_plain_pipe(LevelView L, Common C, StepOpt o)
+{
+    double r_diff = 0.0, r_norm = 0.0;
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    int t = blockIdx.x;
+    float cur[9], nxt[9];
+    float ctau = 0.0f;
+    int cx = 0, cy = 0;
+    auto fetch = [&](int tile, float v[9], float &tau, int &x, int &y) {
+        const int tt = __ldg(&L.tiles[tile]);
+        x = (tt % L.tiles_x) * 32 + lx;
+        y = (tt / L.tiles_x) * 8 + ly;
+        tau = 0.0f;
+        if (x < L.W && y < L.H)
         {
-            float df[9];
-            if (o.direct) load_raw_ro<0>(L, x, y, df);
-            else load_raw_ro<P>(L, x, y, df);
-            SpecialRec none;
-            step_cell<P>(L, C, o, x, y, s, df, tau, false, none, r_diff, r_norm);
+            tau = __ldg(&L.omega[site_of(L, x, y)]);
+            if (tau > 0.0f)
+            {
+                if (o.direct) load_raw_ro<0>(L, x, y, v);
+                else load_raw_ro<P>(L, x, y, v);
+            }
         }
+    };
+    if (t < L.ntiles) fetch(t, cur, ctau, cx, cy);
+    for (; t < L.ntiles; t += gridDim.x)
+    {
+        const int tn = t + gridDim.x;
+        float ntau = 0.0f;
+        int nx = 0, ny = 0;
+        if (tn < L.ntiles) fetch(tn, nxt, ntau, nx, ny);
+        if (ctau > 0.0f)
+        {
+            SpecialRec none;
+            double rd = 0.0, rn = 0.0;
+            step_cell<P>(L, C, o, cx, cy, site_of(L, cx, cy), cur, ctau, false, none, rd, rn);
+            r_diff += rd;
+            r_norm += rn;
+        }
+#pragma unroll
+        for (int q = 0; q < 9; q++) cur[q] = nxt[q];
+        ctau = ntau;
+        cx = nx;
+        cy = ny;
     }
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
@@ -218,7 +273,7 @@ __global__ void __launch_bounds__(128) k_special(LevelView L, Common C, StepOpt 
             load_raw<0>(L, x, y, df);
         else
             load_special<P>(L, C, rec, x, y, df);
-        step_cell<P>(L, C, o, x, y, (int64_t)rec.site, df, rec.tau, true, rec, r_diff, r_norm);
+        step_cell<P>(L, C, o, x, y, (int64_t)rec.site, df, rec.omega, true, rec, r_diff, r_norm);
     }
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
@@ -384,8 +439,7 @@ __global__ void k_set_equilibrium(AllLevels A, Common C, const int32_t *cell_lev
         df[q] = (float)(feq - d2q9::w(q) * (double)C.rho0);
         L.f[(size_t)q * L.plane + s] = df[q];
     }
-    const float tau = L.tau[s];
-    if (tau < 0.0f)
+    if (L.omega[s] < 0.0f)
     {
         const SpecialRec rec = C.specials[L.spec[s]];
         if ((rec.m1 >> 17) & SF_BUFFER)

@@ -96,7 +96,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         lv.W = lv.H = g.n >> (l - 1);
         lv.pitch = ((lv.W + 31) / 32) * 32;
         lv.plane = (int64_t)lv.pitch * lv.H;
-        lv.tau.assign((size_t)lv.plane, 0.0f);
+        lv.omega.assign((size_t)lv.plane, 0.0f);
         lv.spec.assign((size_t)lv.plane, 0u);
         lv.substeps = 1 << (ML - l);
         lv.snapshot_all = g.multiblock;
@@ -174,9 +174,9 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         int l = g.level[c];
         LevelLayout &lv = L.levels[l - 1];
         int s = L.cell_site[c];
-        if (lv.tau[(size_t)s] != 0.0f) throw std::runtime_error("layout: two cells share a site");
-        float tau = (float)g.tau[c];
-        if (!(tau > 0.0f)) throw std::runtime_error("layout: non-positive relaxation time");
+        if (lv.omega[(size_t)s] != 0.0f) throw std::runtime_error("layout: two cells share a site");
+        if (!(g.tau[c] > 0.0)) throw std::runtime_error("layout: non-positive relaxation time");
+        const float omega = (float)(1.0 / g.tau[c]);
         uint32_t flags = 0;
         if (buf_of[c] >= 0) flags |= SF_BUFFER;
         if (p.adsorption && c == g.inlet && g.outlet >= 0) flags |= SF_INLET;
@@ -186,7 +186,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         if (!g.is_buffer[c]) lv.n_active_real++;
         if (!special)
         {
-            lv.tau[(size_t)s] = tau;
+            lv.omega[(size_t)s] = omega;
             continue;
         }
         SpecialRec rec{};
@@ -241,8 +241,8 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             rec.m1 |= (uint32_t)SF_HAS_K << 17;
         }
         rec.site = s;
-        rec.tau = tau;
-        lv.tau[(size_t)s] = -tau;
+        rec.omega = omega;
+        lv.omega[(size_t)s] = -omega;
         L.specials.push_back(rec);
         spec_level.push_back(l);
     }
@@ -278,12 +278,24 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
                 bool any = false;
                 for (int yy = ty * 8; yy < std::min(lv.H, ty * 8 + 8) && !any; yy++)
                     for (int xx = tx * 32; xx < std::min(lv.W, tx * 32 + 32); xx++)
-                        if (lv.tau[(size_t)yy * lv.pitch + xx] != 0.0f)
+                        if (lv.omega[(size_t)yy * lv.pitch + xx] != 0.0f)
                         {
                             any = true;
                             break;
                         }
-                if (any) lv.tile_list.push_back(ty * lv.tiles_x + tx);
+                if (!any) continue;
+                lv.tile_list.push_back(ty * lv.tiles_x + tx);
+                for (int r = 0; r < 8; r++)
+                {
+                    uint32_t m = 0;
+                    int yy = ty * 8 + r;
+                    for (int k = 0; k < 32 && yy < lv.H; k++)
+                    {
+                        int xx = tx * 32 + k;
+                        if (xx < lv.W && lv.omega[(size_t)yy * lv.pitch + xx] > 0.0f) m |= 1u << k;
+                    }
+                    lv.tile_mask.push_back(m);
+                }
             }
     }
 

@@ -11,7 +11,7 @@
 // A cell is "special" when anything but plain streaming feeds its
 // populations: a missing arrival (wall, dropped y-wrap, missing neighbour), a
 // wall link, buffer status (multi-block interface) or an inlet/outlet role.
-// The per-site tau is stored negated for special cells, which then carry a
+// The per-site relaxation rate 1/tau_s is stored negated for special cells, which then carry a
 // 32-byte record with their masks.
 #pragma once
 #include <cstdint>
@@ -56,7 +56,7 @@ struct alignas(16) SpecialRec
     int32_t k_row;     // row of the constant-term table (SF_HAS_K)
     int32_t buf;       // interpolation buffer index (SF_BUFFER), else -1
     int32_t site;      // site of the cell on its level
-    float tau;         // tau_s of the cell
+    float omega;       // 1/tau_s of the cell
 };
 
 struct LevelLayout
@@ -65,9 +65,10 @@ struct LevelLayout
     int W = 0, H = 0;       // sites
     int pitch = 0;          // floats per row (multiple of 32)
     int64_t plane = 0;      // floats per plane
-    std::vector<float> tau;          // per site: 0 inactive, >0 plain, <0 special (|tau| = tau_s)
+    std::vector<float> omega;        // per site 1/tau_s: 0 inactive, >0 plain, <0 special
     std::vector<uint32_t> spec;      // per site: special record index (valid when tau < 0)
     std::vector<int32_t> tile_list;  // active 32x8 tiles: ty * tiles_x + tx
+    std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
     int tiles_x = 0, tiles_y = 0;
     int64_t n_active = 0, n_active_real = 0;
     int substeps = 1;                // per coarse step, 2^(L-l)

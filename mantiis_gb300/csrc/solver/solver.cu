@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <random>
@@ -95,9 +96,10 @@ template <typename T> struct DevBuf
 
 struct LevelDev
 {
-    DevBuf<float> f, tau, tau2, snap, unorm;
+    DevBuf<float> f, omega, tau2, snap, unorm;
     DevBuf<uint32_t> spec;
     DevBuf<int32_t> tiles;
+    DevBuf<uint32_t> tile_mask;
     int64_t steps = 0; // substeps done at this level
 };
 
@@ -122,6 +124,8 @@ struct mgpu_ctx
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    cudaStream_t side_stream = nullptr; // special-cell kernels, forked from / joined to `stream`
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t bytes = 0;
     int64_t launches = 0;
     std::string err;
@@ -138,6 +142,8 @@ struct mgpu_ctx
 
     cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
     int64_t graph_launches = 0;
+    int plain_variant = 0;          // 0: one block per tile, 1: persistent pipelined
+    int sm_count = 1;
     int64_t coarse_done = 0;     // coarse steps executed since creation
     int64_t ref_t = 0;           // reference lb->t
     std::vector<double> residuals;
@@ -186,12 +192,13 @@ struct mgpu_ctx
         const LevelDev &d = lv[l];
         dev::LevelView v{};
         v.f = d.f.p;
-        v.tau = d.tau.p;
+        v.omega = d.omega.p;
         v.spec = d.spec.p;
         v.tau2 = d.tau2.p;
         v.snap = d.snap.p;
         v.unorm = d.unorm.p;
         v.tiles = d.tiles.p;
+        v.tile_mask = d.tile_mask.p;
         v.ntiles = (int)ll.tile_list.size();
         v.tiles_x = ll.tiles_x;
         v.W = ll.W;
@@ -285,21 +292,38 @@ void launch_check(mgpu_ctx *ctx)
 void launch_level(mgpu_ctx *ctx, int l, const dev::LevelView &V, const dev::Common &C, const dev::StepOpt &o)
 {
     const LevelLayout &ll = ctx->lay.levels[l];
+    // fork: the special-cell kernel runs beside the plain-cell kernel (their
+    // slot sets are disjoint under the AA ownership rule)
+    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
     if (!ll.tile_list.empty())
     {
-        dim3 grid((unsigned)ll.tile_list.size()), block(256);
-        if (o.parity == 0) dev::k_plain<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-        else dev::k_plain<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+        if (ctx->plain_variant == 1)
+        {
+            int blocks = std::min((int)ll.tile_list.size(), ctx->sm_count * 4);
+            dim3 grid((unsigned)blocks), block(256);
+            if (o.parity == 0) dev::k_plain_pipe<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_plain_pipe<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+        }
+        else
+        {
+            dim3 grid((unsigned)ll.tile_list.size()), block(256);
+            if (o.parity == 0) dev::k_plain<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_plain<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+        }
         launch_check(ctx);
     }
     if (ll.spec_count)
     {
         int n = (int)ll.spec_count;
         dim3 grid((unsigned)((n + 127) / 128)), block(128);
-        if (o.parity == 0) dev::k_special<0><<<grid, block, 0, ctx->stream>>>(V, C, o, ll.spec_begin, n);
-        else dev::k_special<1><<<grid, block, 0, ctx->stream>>>(V, C, o, ll.spec_begin, n);
+        if (o.parity == 0) dev::k_special<0><<<grid, block, 0, ctx->side_stream>>>(V, C, o, ll.spec_begin, n);
+        else dev::k_special<1><<<grid, block, 0, ctx->side_stream>>>(V, C, o, ll.spec_begin, n);
         launch_check(ctx);
     }
+    // join: the next kernel on the main stream waits for the special cells
+    CK(cudaEventRecord(ctx->ev_join, ctx->side_stream));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
 }
 
 // ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
@@ -522,8 +546,13 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     ctx->lay = build_layout(ctx->grid, lp);
 
     CK(cudaGetDevice(&ctx->device));
+    CK(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device));
+    if (const char *v = std::getenv("MGPU_PLAIN_VARIANT")) ctx->plain_variant = std::atoi(v);
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
+    CK(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     upload_constants();
     cudaStream_t s = ctx->stream;
     int64_t &acct = ctx->bytes;
@@ -534,9 +563,10 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         LevelDev &d = ctx->lv[l];
         d.f.alloc((size_t)ll.plane * 9, acct);
         d.f.zero(s);
-        d.tau.upload(ll.tau, acct, s);
+        d.omega.upload(ll.omega, acct, s);
         d.spec.upload(ll.spec, acct, s);
         d.tiles.upload(ll.tile_list, acct, s);
+        d.tile_mask.upload(ll.tile_mask, acct, s);
         d.unorm.alloc((size_t)ll.plane, acct);
         d.unorm.zero(s);
         if (ll.snapshot_all)
@@ -620,6 +650,10 @@ int mgpu_destroy(mgpu_ctx *ctx)
     if (!ctx) return MGPU_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    if (ctx->side_stream) cudaStreamSynchronize(ctx->side_stream);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MGPU_OK;
