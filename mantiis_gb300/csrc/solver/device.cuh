@@ -34,7 +34,7 @@ struct LevelView
     float *snap;          // 3 * plane: coarse-step-start (drho, ux, uy), may be null
     float *unorm;         // per site |u| of the last stored state, may be null
     float *psi;           // per site pseudopotential (adsorption), may be null
-    float *force;         // 2 * plane: (Fx, Fy) of the current step (adsorption), may be null
+    float *rho_prev;      // per site density at the start of the previous step (adsorption), may be null
     const int32_t *tiles; // active 32x8 tiles
     const uint32_t *tile_mask; // 8 row masks of plain cells per active tile
     int ntiles, tiles_x;
@@ -63,6 +63,7 @@ struct Common
     float psi_rho0;       // rho0 of the exponential form
     float eos_a, eos_b, eos_T; // a_alpha_lu, b_lu, T_lu
     float g_ff, g_fs;
+    int adsorption;       // Shan-Chen step (outputs come from the snapshot planes)
     double *red;          // reduction accumulators
     unsigned int *err;    // device error word
 };
@@ -151,6 +152,20 @@ __device__ __forceinline__ void collide_rmrt(const float df[9], const float feq[
     out[7] = feq[7] + (dt + gp);
     out[6] = feq[6] + (dt - gp);
     out[8] = feq[8] + (dt - gp);
+}
+
+// Pseudopotential (include/coreLB.hpp:515-531): from the lattice Peng-Robinson
+// pressure, psi = sqrt((p_EOS - rho/3) / (3 G_ff)), kept negative (unrooted)
+// where the radicand is negative as the reference does; psi_form 1 is the
+// exponential form rho_psi (1 - exp(-rho / rho_psi)).
+__device__ __forceinline__ float pseudo_potential(float psi_form_exp, float rho_psi, float a, float b, float T,
+                                                  float g_ff, float rho)
+{
+    if (psi_form_exp != 0.0f) return rho_psi * (1.0f - expf(-rho / rho_psi));
+    const float md = rho; // molar density, Mw_lu = 1
+    const float p = md * T / (1.0f - b * md) - a * md * md / (1.0f + 2.0f * b * md - b * b * md * md);
+    const float acc = (p - rho * (1.0f / 3.0f)) / (3.0f * g_ff);
+    return acc < 0.0f ? acc : sqrtf(acc);
 }
 
 // Moment matrix M and its inverse (include/globalParameters.hpp:154-175).
@@ -332,7 +347,7 @@ __device__ __forceinline__ void load_special(const LevelView &L, const Common &C
     float raw[9];
     load_raw<P>(L, x, y, raw);
     const uint32_t arrive = rec.m0 & 0x1FFu, over = (rec.m0 >> 9) & 0x1FFu, wall = (rec.m0 >> 18) & 0x1FFu;
-    const uint32_t quirk = rec.m1 & 0x1FFu, bnd = (rec.m1 >> 9) & 0xFFu, flags = rec.m1 >> 17;
+    const uint32_t quirk = rec.m1 & 0x1FFu, bnd = (rec.m1 >> 9) & 0xFFu, flags = (rec.m1 >> 17) & 0xFu;
 #pragma unroll
     for (int q = 0; q < 9; q++) df[q] = ((arrive >> q) & 1u) ? raw[q] : 0.0f;
     if (wall)

@@ -70,7 +70,7 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
         return om;
     }
     rec = C.specials[L.spec[s]];
-    const uint32_t flags = rec.m1 >> 17;
+    const uint32_t flags = (rec.m1 >> 17) & 0xFu;
     if ((flags & SF_BUFFER) && (first_sub || direct))
     {
 #pragma unroll
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(128) k_special(LevelView L, Common C, StepOpt 
         const SpecialRec rec = C.specials[begin + i];
         const int x = rec.site % L.pitch, y = rec.site / L.pitch;
         float df[9];
-        const uint32_t flags = rec.m1 >> 17;
+        const uint32_t flags = (rec.m1 >> 17) & 0xFu;
         if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
         {
 #pragma unroll
@@ -276,6 +276,132 @@ __global__ void __launch_bounds__(128) k_special(LevelView L, Common C, StepOpt 
         step_cell<P>(L, C, o, x, y, (int64_t)rec.site, df, rec.omega, true, rec, r_diff, r_norm);
     }
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+}
+
+// Maximum of a non-negative double over the block, then one atomic per block
+// (non-negative doubles order like their bit patterns).
+__device__ __forceinline__ void block_max(double v, double *dst)
+{
+    __shared__ double sm[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    if (wid == 0)
+    {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? sm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0)
+            atomicMax(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__double_as_longlong(v));
+    }
+    __syncthreads();
+}
+
+// Adsorption, first pass of a step (include/mantiisApp.hpp:248-252,
+// include/coreLB.hpp:1056-1067, 515-531, 1269-1283): density of every cell from
+// its streamed populations, its pseudopotential, and the relative density change
+// since the previous step (maximum over the cells).
+template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
+{
+    const int tile = L.tiles[blockIdx.x];
+    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
+    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    double rmax = 0.0;
+    if (x < L.W && y < L.H && L.omega[site_of(L, x, y)] != 0.0f)
+    {
+        const int64_t s = site_of(L, x, y);
+        float df[9];
+        bool special;
+        SpecialRec rec;
+        load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
+        float drho = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) drho += df[q];
+        const float rho = C.rho0 + drho;
+        L.psi[s] = pseudo_potential((float)C.psi_form, C.psi_rho0, C.eos_a, C.eos_b, C.eos_T, C.g_ff, rho);
+        const float old = L.rho_prev[s];
+        rmax = (double)(fabsf(rho - old) / old);
+        L.rho_prev[s] = rho;
+    }
+    if (o.diff) block_max(rmax, C.red + o.red_slot);
+}
+
+// Adsorption, second pass: Shan-Chen force (include/coreLB.hpp:533-566),
+// velocity with the half-force shift (:1069-1099), equilibrium, plain MRT
+// (:694-742), Guo source term (:568-630), AA store.  Bounce-back walls, the
+// x-periodic links and the inlet/outlet overwrite (:859-865, 969-1009) are
+// applied when the populations are read in the next step.
+template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
+{
+    const int tile = L.tiles[blockIdx.x];
+    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
+    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    if (x >= L.W || y >= L.H) return;
+    const int64_t s = site_of(L, x, y);
+    if (L.omega[s] == 0.0f) return;
+    float df[9];
+    bool special;
+    SpecialRec rec;
+    const float omega = load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
+    const uint32_t out = special ? ((rec.m1 >> 21) & 0x1FFu) : 0x1FFu;
+    const uint32_t wall = special ? ((rec.m0 >> 18) & 0x1FFu) : 0u;
+    // sum over the streaming links of w_f psi(x + c) c, formed from psi differences
+    const float psx = L.psi[s];
+    float sx = 0.f, sy = 0.f, cwx = 0.f, cwy = 0.f, wwx = 0.f, wwy = 0.f;
+#pragma unroll
+    for (int q = 1; q < 9; q++)
+    {
+        const float w = (float)d2q9::wf(q);
+        if ((out >> q) & 1u)
+        {
+            const int xn = wrapx(x + d2q9::cx(q), L.W), yn = wrapx(y + d2q9::cy(q), L.H);
+            const float dpsi = L.psi[site_of(L, xn, yn)] - psx;
+            sx += w * dpsi * (float)d2q9::cx(q);
+            sy += w * dpsi * (float)d2q9::cy(q);
+            cwx += w * (float)d2q9::cx(q);
+            cwy += w * (float)d2q9::cy(q);
+        }
+        if ((wall >> q) & 1u)
+        {
+            wwx += w * (float)d2q9::cx(q);
+            wwy += w * (float)d2q9::cy(q);
+        }
+    }
+    const float kff = -6.0f * C.g_ff * psx;
+    const float Fx = kff * (sx + psx * cwx) - C.g_fs * psx * psx * wwx + C.fbody;
+    const float Fy = kff * (sy + psx * cwy) - C.g_fs * psx * psx * wwy;
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+    {
+        drho += df[q];
+        jx += (float)d2q9::cx(q) * df[q];
+        jy += (float)d2q9::cy(q) * df[q];
+    }
+    const float rho = C.rho0 + drho;
+    const float ux = (jx + 0.5f * Fx) / rho, uy = (jy + 0.5f * Fy) / rho;
+    if (o.snap_store)
+    {
+        L.snap[s] = drho;
+        L.snap[L.plane + s] = ux;
+        L.snap[2 * L.plane + s] = uy;
+    }
+    float feq[9], fs[9];
+    equilibrium(drho, rho, ux, uy, feq);
+    const float tau_s = 1.0f / omega, tau_d = L.tau2[s];
+    collide_mrt(df, feq, tau_s, tau_d, fs);
+    add_source(fs, ux, uy, Fx, Fy, tau_s, tau_d);
+    if (special && (rec.m1 & 0x1FFu))
+    {
+        const uint32_t quirk = rec.m1 & 0x1FFu;
+        float *side_now = C.side + (size_t)P * C.n_quirk;
+        int qi = 0;
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
+    }
+    store_post<P>(L, x, y, fs);
 }
 
 // Reads the current state of every reference cell (no update): FP64 density,
@@ -319,14 +445,22 @@ __global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int3
             jx += (double)d2q9::cx(q) * (double)df[q];
             jy += (double)d2q9::cy(q) * (double)df[q];
         }
-        const double r = (double)C.rho0 + ddr;
-        const double vx = (jx + (double)L.fshift) / r, vy = jy / r;
+        double r = (double)C.rho0 + ddr;
+        double vx = (jx + (double)L.fshift) / r, vy = jy / r;
+        if (C.adsorption)
+        {
+            // the reference reports the density and velocity computed at the
+            // start of the last step (include/mantiisApp.hpp:248-265)
+            r = (double)C.rho0 + (double)L.snap[s];
+            vx = (double)L.snap[L.plane + s];
+            vy = (double)L.snap[2 * L.plane + s];
+        }
         if (rho_out) rho_out[c] = r;
         if (ux_out) ux_out[c] = vx;
         if (uy_out) uy_out[c] = vy;
         if (f_out)
             for (int q = 0; q < 9; q++) f_out[c * 9 + q] = d2q9::w(q) * (double)C.rho0 + (double)df[q];
-        const bool buffer = special && ((rec.m1 >> 17) & SF_BUFFER);
+        const bool buffer = special && (((rec.m1 >> 17) & 0xFu) & SF_BUFFER);
         if (!buffer)
         {
             const double area = (double)(1 << (2 * l));
@@ -439,10 +573,24 @@ __global__ void k_set_equilibrium(AllLevels A, Common C, const int32_t *cell_lev
         df[q] = (float)(feq - d2q9::w(q) * (double)C.rho0);
         L.f[(size_t)q * L.plane + s] = df[q];
     }
+    if (L.rho_prev)
+    {
+        // the same FP32 sum as the first step's density, so an unchanged state
+        // reads as no change
+        float drho = 0.0f;
+        for (int q = 0; q < 9; q++) drho += df[q];
+        L.rho_prev[s] = C.rho0 + drho;
+    }
+    if (L.snap)
+    {
+        L.snap[s] = (float)(r - (double)C.rho0);
+        L.snap[L.plane + s] = (float)vx;
+        L.snap[2 * L.plane + s] = (float)vy;
+    }
     if (L.omega[s] < 0.0f)
     {
         const SpecialRec rec = C.specials[L.spec[s]];
-        if ((rec.m1 >> 17) & SF_BUFFER)
+        if (((rec.m1 >> 17) & 0xFu) & SF_BUFFER)
             for (int q = 0; q < 9; q++) C.ibuf[(size_t)q * C.n_buf + rec.buf] = df[q];
     }
 }

@@ -97,6 +97,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         lv.pitch = ((lv.W + 31) / 32) * 32;
         lv.plane = (int64_t)lv.pitch * lv.H;
         lv.omega.assign((size_t)lv.plane, 0.0f);
+        if (p.adsorption) lv.tau_d.assign((size_t)lv.plane, 0.0f);
         lv.spec.assign((size_t)lv.plane, 0u);
         lv.substeps = 1 << (ML - l);
         lv.snapshot_all = g.multiblock;
@@ -124,7 +125,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
     };
 
     // masks from the reference link lists
-    std::vector<uint32_t> arrive(N, 0), over(N, 0), wall(N, 0), quirk(N, 0);
+    std::vector<uint32_t> arrive(N, 0), over(N, 0), wall(N, 0), quirk(N, 0), out(N, 0);
     for (size_t k = 0; k < g.stream_id.size(); k++)
     {
         int64_t src = g.stream_id[k], dst = g.stream_loc[k];
@@ -132,6 +133,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         if (torus_site(src, q) != L.cell_site[dst] || g.level[src] != g.level[dst])
             throw std::runtime_error("layout: stream link does not land on its torus neighbour");
         arrive[dst] |= 1u << q;
+        out[src] |= 1u << q;
     }
     for (size_t k = 0; k < g.per_id.size(); k++)
     {
@@ -141,6 +143,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             throw std::runtime_error("layout: periodic link does not land on its torus neighbour");
         arrive[dst] |= 1u << q;
         over[dst] |= 1u << q;
+        out[src] |= 1u << q;
     }
     for (size_t k = 0; k < g.wall_id.size(); k++)
     {
@@ -181,7 +184,13 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         if (buf_of[c] >= 0) flags |= SF_BUFFER;
         if (p.adsorption && c == g.inlet && g.outlet >= 0) flags |= SF_INLET;
         if (p.adsorption && c == g.outlet && g.inlet >= 0) flags |= SF_OUTLET;
-        bool special = arrive[c] != ALL || wall[c] != 0 || flags != 0;
+        bool special = arrive[c] != ALL || wall[c] != 0 || flags != 0 || (p.adsorption && out[c] != ALL);
+        if (p.adsorption)
+        {
+            // include/coreLB.hpp:710 (tau_d of the plain MRT from the cell's Kn)
+            double a = p.mfp_over_cl * 1.0 / (1.0 + 2.0 * g.kn[c]);
+            lv.tau_d[(size_t)s] = (float)(0.5 + (3.0 / 2.0) * std::sqrt(3.0) * 1.0 / std::pow((1.0 / std::sqrt(a)) * 2.0, 2.0));
+        }
         lv.n_active++;
         if (!g.is_buffer[c]) lv.n_active_real++;
         if (!special)
@@ -192,7 +201,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         SpecialRec rec{};
         int b = g.bnd[c];
         rec.m0 = arrive[c] | (over[c] << 9) | (wall[c] << 18);
-        rec.m1 = quirk[c] | ((uint32_t)(b < 0 ? 0xFF : b) << 9) | (flags << 17);
+        rec.m1 = quirk[c] | ((uint32_t)(b < 0 ? 0xFF : b) << 9) | (flags << 17) | (out[c] << 21);
         double kn = g.kn[c];
         double r = 0.0;
         if (wall[c])

@@ -49,8 +49,10 @@ struct alignas(16) SpecialRec
                        //   arrive bit p: f_p streams in from the neighbour at -c_p
                        //   override bit p: that arrival is x-periodic (it wins over walls)
                        //   wall bit q: link q of this cell is a wall link
-    uint32_t m1;       // quirk mask | boundary type << 9 (8 bits, 0xFF = none) | flags << 17
+    uint32_t m1;       // quirk mask | boundary type << 9 (8 bits, 0xFF = none) | flags << 17 (4 bits)
+                       //   | out mask << 21
                        //   quirk bit q: wall link whose neighbour site is an active cell
+                       //   out bit q: link q streams (or wraps in x) to a live neighbour
     float r;           // wall coefficient (SRBB / MDBB), from the cell's Kn
     int32_t quirk_base;// side-buffer slot of this cell's first quirk link
     int32_t k_row;     // row of the constant-term table (SF_HAS_K)
@@ -66,6 +68,7 @@ struct LevelLayout
     int pitch = 0;          // floats per row (multiple of 32)
     int64_t plane = 0;      // floats per plane
     std::vector<float> omega;        // per site 1/tau_s: 0 inactive, >0 plain, <0 special
+    std::vector<float> tau_d;        // per site tau_d of the plain MRT (adsorption), else empty
     std::vector<uint32_t> spec;      // per site: special record index (valid when tau < 0)
     std::vector<int32_t> tile_list;  // active 32x8 tiles: ty * tiles_x + tx
     std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
@@ -111,6 +114,7 @@ struct LayoutParams
     int collision = COLL_RMRT;
     double rho0 = 0.0;   // reference density of the deviation storage (= initial density)
     bool adsorption = false;
+    double mfp_over_cl = 0.0; // mean free path / lattice spacing (tau_d of the plain MRT)
 };
 
 struct ImageLayout

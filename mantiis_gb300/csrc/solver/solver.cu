@@ -96,7 +96,7 @@ template <typename T> struct DevBuf
 
 struct LevelDev
 {
-    DevBuf<float> f, omega, tau2, snap, unorm;
+    DevBuf<float> f, omega, tau2, snap, unorm, psi, rho_prev;
     DevBuf<uint32_t> spec;
     DevBuf<int32_t> tiles;
     DevBuf<uint32_t> tile_mask;
@@ -139,6 +139,7 @@ struct mgpu_ctx
     DevBuf<double> out_rho, out_ux, out_uy, out_f;
     DevBuf<unsigned int> errword;
     float rho0f = 0.f;
+    bool adsorption = false; // Shan-Chen step body (include/mantiisApp.hpp:248-265)
 
     cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
     int64_t graph_launches = 0;
@@ -172,8 +173,9 @@ struct mgpu_ctx
         C.rho0 = rho0f;
         C.inlet_axis = (float)(d2q9::W[1] * units.rhoin - d2q9::W[1] * (double)rho0f);
         C.inlet_diag = (float)(d2q9::W[2] * units.rhoin - d2q9::W[5] * (double)rho0f);
-        C.wall = prm.wall;
-        C.collision = prm.collision;
+        C.wall = adsorption ? WALL_BB : prm.wall;
+        C.collision = adsorption ? COLL_MRT : prm.collision;
+        C.adsorption = adsorption ? 1 : 0;
         C.fbody = (float)prm.fbody;
         C.psi_form = prm.psi_form;
         C.psi_rho0 = (float)prm.rho_psi;
@@ -197,6 +199,8 @@ struct mgpu_ctx
         v.tau2 = d.tau2.p;
         v.snap = d.snap.p;
         v.unorm = d.unorm.p;
+        v.psi = d.psi.p;
+        v.rho_prev = d.rho_prev.p;
         v.tiles = d.tiles.p;
         v.tile_mask = d.tile_mask.p;
         v.ntiles = (int)ll.tile_list.size();
@@ -331,6 +335,32 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
 {
     const int L = ctx->lay.max_level;
     dev::Common C = ctx->common();
+    if (ctx->adsorption)
+    {
+        // single level: density and pseudopotential of every cell first (the
+        // force needs the neighbours'), then the collision and streaming
+        const LevelLayout &ll = ctx->lay.levels[0];
+        dev::LevelView V = ctx->view(0);
+        dev::StepOpt o{};
+        o.parity = (int)(ctx->lv[0].steps & 1);
+        o.direct = ctx->lv[0].steps == 0 ? 1 : 0;
+        o.diff = diff ? 1 : 0;
+        o.red_slot = red_slot;
+        o.snap_store = 1;
+        dim3 grid((unsigned)ll.tile_list.size()), block(256);
+        if (!ll.tile_list.empty())
+        {
+            if (o.parity == 0) dev::k_ads_psi<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_ads_psi<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            launch_check(ctx);
+            if (o.parity == 0) dev::k_ads_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            else dev::k_ads_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            launch_check(ctx);
+        }
+        ctx->lv[0].steps++;
+        ctx->coarse_done++;
+        return;
+    }
     const bool mb = ctx->grid.multiblock;
     for (int l = L - 1; l >= 0; l--)
     {
@@ -464,6 +494,16 @@ void run_batch_with_residuals(mgpu_ctx *ctx, int n)
 {
     int64_t k0 = ctx->coarse_done;
     zero_slots(ctx, (int)((k0 + 1) % kRing), n);
+    if (ctx->adsorption)
+    {
+        // the density change of step k is known within step k
+        for (int i = 0; i < n; i++)
+        {
+            int64_t k = ctx->coarse_done + 1;
+            coarse_step(ctx, true, false, (int)((k % kRing) * 4));
+        }
+        return;
+    }
     for (int i = 0; i < n; i++)
     {
         int64_t k = ctx->coarse_done + 1; // this step
@@ -475,10 +515,21 @@ void run_batch_with_residuals(mgpu_ctx *ctx, int n)
     cells_pass(ctx, nullptr, nullptr, nullptr, nullptr, true, false, (int)((last % kRing) * 4));
 }
 
-void transport_only(mgpu_ctx *ctx)
+// residual of one step from its accumulator slot: transport
+// sum|d|u|| / sum|u| (include/coreLB.hpp:1248-1267), adsorption max relative
+// density change, 1e-5 when below 1e-15 (include/coreLB.hpp:1269-1283)
+double residual_of(const mgpu_ctx *ctx, const double *v)
 {
-    if (ctx->prm.simulation != MGPU_SIM_TRANSPORT)
-        throw std::runtime_error("this build of the solver runs the transport simulation only");
+    if (ctx->adsorption) return v[0] < 1.0e-15 ? 1.0e-5 : v[0];
+    return v[0] / v[1];
+}
+
+void check_supported(mgpu_ctx *ctx)
+{
+    if (ctx->prm.simulation == MGPU_SIM_COUPLED)
+        throw std::runtime_error("the coupled simulation is not available in this build");
+    if (ctx->prm.simulation == MGPU_SIM_ADSORPTION && ctx->grid.max_level > 1)
+        throw std::runtime_error("the adsorption step is single-block (include/mantiisApp.hpp:248-265 steps level 1 only)");
 }
 } // namespace
 
@@ -534,7 +585,8 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     go.edge_fine = p->edge_fine != 0;
     ctx->grid = build_grid(img, go);
     if (ctx->grid.max_level > dev::kMaxLevels) throw std::runtime_error("too many refinement levels");
-    transport_only(ctx.get());
+    ctx->adsorption = p->simulation == MGPU_SIM_ADSORPTION;
+    check_supported(ctx.get());
 
     double rho_init = p->rho_init > 0 ? p->rho_init : ctx->units.rhoin;
     ctx->rho0f = (float)rho_init;
@@ -543,6 +595,13 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     lp.collision = p->collision;
     lp.rho0 = (double)ctx->rho0f;
     lp.adsorption = p->simulation != MGPU_SIM_TRANSPORT;
+    lp.mfp_over_cl = ctx->units.mfp / ctx->units.Cl;
+    if (lp.adsorption)
+    {
+        // the adsorption loop calls the plain MRT and bounce-back directly
+        lp.wall = WALL_BB;
+        lp.collision = COLL_MRT;
+    }
     ctx->lay = build_layout(ctx->grid, lp);
 
     CK(cudaGetDevice(&ctx->device));
@@ -569,10 +628,18 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         d.tile_mask.upload(ll.tile_mask, acct, s);
         d.unorm.alloc((size_t)ll.plane, acct);
         d.unorm.zero(s);
-        if (ll.snapshot_all)
+        if (ll.snapshot_all || ctx->adsorption)
         {
             d.snap.alloc((size_t)ll.plane * 3, acct);
             d.snap.zero(s);
+        }
+        if (ctx->adsorption)
+        {
+            d.tau2.upload(ll.tau_d, acct, s);
+            d.psi.alloc((size_t)ll.plane, acct);
+            d.psi.zero(s);
+            d.rho_prev.alloc((size_t)ll.plane, acct);
+            d.rho_prev.zero(s);
         }
     }
     ctx->specials.upload(ctx->lay.specials, acct, s);
@@ -702,7 +769,7 @@ int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
             int stop = -1;
             for (int i = 0; i < batch; i++)
             {
-                double d = slots[(size_t)i * 4] / slots[(size_t)i * 4 + 1];
+                double d = residual_of(ctx, &slots[(size_t)i * 4]);
                 ctx->residuals.push_back(d);
                 if (d < tol)
                 {
@@ -745,12 +812,21 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
             std::vector<double> v(pending.size() * 4);
             for (size_t i = 0; i < pending.size(); i++) read_slot(ctx, (int)pending[i], &v[i * 4]);
             CK(cudaStreamSynchronize(ctx->stream));
-            for (size_t i = 0; i < pending.size(); i++) ctx->residuals.push_back(v[i * 4] / v[i * 4 + 1]);
+            for (size_t i = 0; i < pending.size(); i++) ctx->residuals.push_back(residual_of(ctx, &v[i * 4]));
             pending.clear();
         };
         for (int i = 0; i < n_steps; i++)
         {
             int64_t k = ctx->coarse_done + 1;
+            if (ctx->adsorption)
+            {
+                bool diff = (k % K == 0);
+                if (diff) zero_slots(ctx, (int)(k % kRing), 1);
+                coarse_step(ctx, diff, false, (int)((k % kRing) * 4));
+                if (diff) pending.push_back(k);
+                if ((int)pending.size() >= kRing / 2) flush();
+                continue;
+            }
             // residual of step s is evaluated by kernel s+1 against |u| stored by kernel s
             bool diff = k >= 2 && ((k - 1) % K == 0);
             bool store = (k % K == 0);

@@ -1,0 +1,71 @@
+"""GPU parity of the adsorption step (Shan-Chen pseudopotential force, plain
+MRT with the Guo source, bounce-back walls, x-periodic links and the
+generalized inlet/outlet) against the reference's gold files and the FP64
+oracle.  The 100-step adsorption transient is strongly nonlinear (density
+0.11-1.35, |u| up to 0.19); tolerances are stated per test."""
+import numpy as np
+import pytest
+from conftest import load
+
+from mantiis_gb300 import SIM_ADSORPTION, HostGrid, Solver, default_params, generate_disks
+from oracle.pyoracle import for_grid
+from test_gpu_transport import record
+
+pytestmark = pytest.mark.gpu
+
+
+def test_adsorption_gold_64(fixture64):
+    # test/run_tests.sh adsorption case: dx = 12 nm, 64x64, 100 steps
+    p = default_params(dx=12e-9, simulation=SIM_ADSORPTION)
+    s = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    assert s.run(100) == 100
+    px = s.pixels()
+    umax = np.abs(fixture64["adsorption_ux"]).max()
+    e_ux = np.abs(px["ux"] - fixture64["adsorption_ux"]).max() / umax
+    e_uy = np.abs(px["uy"] - fixture64["adsorption_uy"]).max() / umax
+    e_rho = np.abs(px["rho"] - fixture64["adsorption_rho"]).max() / np.abs(fixture64["adsorption_rho"]).max()
+    record("adsorption_gold_64", ux=e_ux, uy=e_uy, rho=e_rho)
+    assert e_ux < 1e-3 and e_uy < 1e-3 and e_rho < 1e-4
+
+
+def test_adsorption_residuals_vs_oracle(fixture64):
+    p = default_params(dx=12e-9, simulation=SIM_ADSORPTION)
+    g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    o = for_grid(g, sim="adsorption", dx=12e-9)
+    o.run(60)
+    ref = o.residuals()
+    s = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    s.run(60)
+    r = s.residuals()
+    assert len(r) == 60 and r[0] == 1e-5 == ref[0]
+    e = np.abs(r - ref) / ref
+    record("adsorption_residuals_64", max_rel=e.max(), median_rel=np.median(e))
+    assert np.median(e) < 1e-3
+
+
+def test_exponential_pseudopotential_vs_oracle():
+    # the exponential form psi = rho0 (1 - exp(-rho/rho0)) with G = -4.5 and
+    # G_ads = -0.5 in the common Shan-Chen convention (weights 1/9, 1/36), initial
+    # density 0.5 +- 1e-3.  The reference's force carries -6 G_ff with weights
+    # 1/3, 1/12 (18 x the common one) and -G_fs with weights 1/3, 1/12, so
+    # G_ff = G / 18 and G_fs = 3 G_ads.
+    n = 128
+    pore = generate_disks(n, 4, 10, 0.6, 3001)
+    kn = np.where(pore == 1, 0.1, 0.0)
+    lp = np.where(pore == 1, 7.73, 0.0)
+    kw = dict(psi_form=1, rho_psi=0.5, g_ff=-4.5 / 18, g_fs=-1.5)
+    p = default_params(dx=1e-9, simulation=SIM_ADSORPTION, rho_init=0.5, fbody=0.0, **kw)
+    g = HostGrid(pore, kn, lp, p)
+    rng = np.random.default_rng(3)
+    rho = 0.5 + rng.uniform(-1e-3, 1e-3, g.n_cells)
+    o = for_grid(g, sim="adsorption", dx=1e-9, fbody=0.0, rho_init=rho, **kw)
+    o.run(50)
+    ref = o.fields()
+    s = Solver(pore, kn, lp, p)
+    s.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
+    s.run(50)
+    got = s.cells()
+    e_rho = np.abs(got["rho"] - ref["rho"]).max() / 0.5
+    e_ux = np.abs(got["ux"] - ref["ux"]).max() / max(np.abs(ref["ux"]).max(), 1e-30)
+    record("adsorption_exponential_128", rho=e_rho, ux=e_ux)
+    assert e_rho < 1e-6 and e_ux < 1e-3
