@@ -155,6 +155,23 @@ int mgpu_reconstructed(const mgpu_ctx *ctx, int64_t *out);
  * reference cell order. */
 int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy);
 
+/* mgpu_set_equilibrium without any allocation; it has no counterpart in the
+ * reference.  For callers that must not allocate device or host memory during a
+ * run, e.g. a loop that warm-starts contexts while other contexts keep stepping
+ * on their own streams (cudaFree synchronizes the whole device), or a process
+ * whose device memory is owned by another allocator.  Same arguments, result and
+ * error codes as mgpu_set_equilibrium; the inputs are staged through one static
+ * device array of MGPU_NOALLOC_MAX_CELLS cells (24 MiB, part of the library's
+ * module image), so a grid with more cells is rejected with MGPU_E_ARG.
+ * - The context's device must be current.
+ * - The first call on a device looks up the array's address (and may load the
+ *   module); make it before any stream capture.
+ * - All contexts on a device share the array: calls that overlap in time (from
+ *   several host threads) race.  Each call returns after its kernel has read the
+ *   array, so calls made one after another are safe. */
+#define MGPU_NOALLOC_MAX_CELLS (1 << 20)
+int mgpu_set_equilibrium_noalloc(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy);
+
 /* Use an external cudaStream_t for all work of this context (NULL = own stream). */
 int mgpu_set_stream(mgpu_ctx *ctx, void *stream);
 

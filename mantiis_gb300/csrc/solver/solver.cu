@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -1044,6 +1045,72 @@ int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, con
         dev::k_set_equilibrium<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
             ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, dr.p, du.p, dv.p);
         launch_check(ctx);
+        CK(cudaStreamSynchronize(ctx->stream));
+        return MGPU_OK;
+    });
+}
+
+} // extern "C"
+
+namespace
+{
+// Staging area of mgpu_set_equilibrium_noalloc: rho, u_x, u_y of up to
+// MGPU_NOALLOC_MAX_CELLS cells (3 x 8 MiB), part of the module image, so it exists
+// once per device and no call allocates it.  Nothing in it has to start at zero:
+// each call writes the 3 n values its kernel reads before the kernel runs.
+__device__ __align__(256) double g_noalloc_stage[3 * (size_t)MGPU_NOALLOC_MAX_CELLS];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kMaxDevices] = {};
+
+// the array's device address on `device`, looked up once per device with that
+// device current (the first lookup may load the module)
+double *noalloc_stage(int device)
+{
+    if (device < 0 || device >= kMaxDevices) throw std::invalid_argument("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device])
+    {
+        int prev = -1;
+        CK(cudaGetDevice(&prev));
+        if (prev != device) CK(cudaSetDevice(device));
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_stage);
+        if (prev != device) CK(cudaSetDevice(prev));
+        CK(e);
+        g_noalloc_ptr[device] = static_cast<double *>(p);
+    }
+    return g_noalloc_ptr[device];
+}
+} // namespace
+
+extern "C" {
+
+int mgpu_set_equilibrium_noalloc(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || !rho || !ux || !uy) throw std::invalid_argument("null argument");
+        const int64_t n = ctx->grid.n_cells;
+        if (n > MGPU_NOALLOC_MAX_CELLS)
+            throw std::length_error("mgpu_set_equilibrium_noalloc: " + std::to_string(n) +
+                                        " cells exceed the static staging area of " +
+                                        std::to_string(MGPU_NOALLOC_MAX_CELLS) + " cells");
+        int prev = -1;
+        CK(cudaGetDevice(&prev));
+        if (prev != ctx->device)
+            throw std::logic_error("mgpu_set_equilibrium_noalloc: the context's device is not current");
+        double *stage = noalloc_stage(ctx->device);
+        if (n == 0) return MGPU_OK;
+        double *dr = stage, *du = stage + MGPU_NOALLOC_MAX_CELLS, *dv = stage + 2 * (size_t)MGPU_NOALLOC_MAX_CELLS;
+        CK(cudaMemcpyAsync(dr, rho, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(du, ux, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(dv, uy, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        for (auto &l : ctx->lv) l.steps = 0;
+        dev::k_set_equilibrium<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, dr, du, dv);
+        launch_check(ctx);
+        // the staging area is free for the next call once this returns
         CK(cudaStreamSynchronize(ctx->stream));
         return MGPU_OK;
     });

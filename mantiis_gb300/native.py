@@ -13,6 +13,7 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libmantiis_gpu.so"
 
 SIM_TRANSPORT, SIM_ADSORPTION, SIM_COUPLED = 0, 1, 2
+NOALLOC_MAX_CELLS = 1 << 20  # MGPU_NOALLOC_MAX_CELLS
 
 
 class Params(C.Structure):
@@ -89,6 +90,7 @@ SIGNATURES = {
     "mgpu_observables": (C.c_int, [P, F64P]),
     "mgpu_reconstructed": (C.c_int, [P, I64P]),
     "mgpu_set_equilibrium": (C.c_int, [P, F64P, F64P, F64P]),
+    "mgpu_set_equilibrium_noalloc": (C.c_int, [P, F64P, F64P, F64P]),
     "mgpu_set_stream": (C.c_int, [P, P]),
     "mgpu_launch_count": (C.c_int64, [P]),
     "mgpu_last_error": (C.c_char_p, [P]),
@@ -325,6 +327,12 @@ class Solver:
     def set_equilibrium(self, rho, ux, uy):
         a = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in (rho, ux, uy)]
         self._check(lib().mgpu_set_equilibrium(self._h, *a))
+
+    def set_equilibrium_noalloc(self, rho, ux, uy):
+        """set_equilibrium staged through the library's static device array
+        (mgpu_set_equilibrium_noalloc): no allocation, at most NOALLOC_MAX_CELLS cells."""
+        a = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in (rho, ux, uy)]
+        self._check(lib().mgpu_set_equilibrium_noalloc(self._h, *a))
 
     def set_stream(self, stream_handle):
         self._check(lib().mgpu_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
