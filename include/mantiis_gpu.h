@@ -178,6 +178,25 @@ int mgpu_set_stream(mgpu_ctx *ctx, void *stream);
 /* Number of kernel launches issued by this context so far. */
 int64_t mgpu_launch_count(const mgpu_ctx *ctx);
 
+/* ---- batched stepping (no reference counterpart: the reference runs one
+ * image per process, include/mantiisApp.hpp:286-430) ----
+ * A batch steps a group of transport contexts of the current device together:
+ * each phase of a coarse step is one launch over every image, each interface
+ * wave one launch, two coarse steps are replayed from one CUDA graph.  The
+ * contexts keep their state and stay usable on their own; batch work is
+ * ordered after earlier work on each context's stream and before later work.
+ * A context must not be stepped by two batches at once. */
+typedef struct mgpu_batch mgpu_batch;
+int mgpu_batch_create(mgpu_ctx *const *ctxs, int n, mgpu_batch **out);
+/* n coarse steps of every image, no residual; enqueues and returns */
+int mgpu_batch_advance(mgpu_batch *b, int n_steps);
+/* mgpu_observables of every image, 4 values per image */
+int mgpu_batch_observables(mgpu_batch *b, double *out);
+int mgpu_batch_set_stream(mgpu_batch *b, void *stream);
+int mgpu_batch_sync(mgpu_batch *b);
+int64_t mgpu_batch_launch_count(const mgpu_batch *b);
+int mgpu_batch_destroy(mgpu_batch *b);
+
 const char *mgpu_last_error(const mgpu_ctx *ctx);
 const char *mgpu_global_error(void);
 

@@ -7,6 +7,7 @@ from .native import (  # noqa: F401
     SIM_ADSORPTION,
     SIM_COUPLED,
     SIM_TRANSPORT,
+    Batch,
     HostGrid,
     MantiisError,
     Solver,
@@ -19,6 +20,7 @@ from .native import (  # noqa: F401
 
 __all__ = [
     "Solver",
+    "Batch",
     "HostGrid",
     "MantiisError",
     "default_params",

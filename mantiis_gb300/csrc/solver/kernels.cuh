@@ -88,21 +88,21 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
 // regularized MRT / MRT / BGK collision, the wall values of special cells and
 // the AA-pattern store (include/coreLB.hpp:420-430, 646-792, 834-977, 1018-1054).
 template <int P>
-__device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y, int64_t s,
-                                          const float df[9], float omega, bool special, const SpecialRec &rec,
-                                          double &r_diff, double &r_norm, bool interior = false)
+__device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int diff, int store_u,
+                                          int x, int y, int64_t s, const float df[9], float omega, bool special,
+                                          const SpecialRec &rec, double &r_diff, double &r_norm, bool interior = false)
 {
     float drho, rho, ux, uy;
     macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
-    if (o.diff | o.store_u)
+    if (diff | store_u)
     {
         const float un = sqrtf(ux * ux + uy * uy);
-        if (o.diff)
+        if (diff)
         {
             r_diff = (double)fabsf(un - L.unorm[s]);
             r_norm = (double)un;
         }
-        if (o.store_u) L.unorm[s] = un;
+        if (store_u) L.unorm[s] = un;
     }
     if (o.snap_store)
     {
@@ -171,111 +171,128 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
     store_post<P>(L, x, y, fs, interior);
 }
 
-// Plain cells of one level (all nine populations stream in, no wall link):
-// one thread per site, 32x8 sites per block, blocks over the active tiles.
-// Each slot a thread reads is written by that thread alone in this launch (AA
-// ownership), so the loads take the read-only path.
-template <int P> __global__ void __launch_bounds__(256, 6) k_plain(LevelView L, Common C, StepOpt o)
+// Plain cells of one active tile (all nine populations stream in, no wall
+// link): one thread per site of a 32x8 tile, the row masks of plain cells let
+// the relaxation rate and the nine populations load together.  Each slot a
+// thread reads is written by that thread alone in this launch (AA ownership),
+// so the loads take the read-only path.
+template <int P>
+__device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, const StepOpt &o, int t, int diff,
+                                           int store_u, double &r_diff, double &r_norm)
 {
-    // the tile id and this row's plain-cell mask are independent loads, so the
-    // relaxation rate and the populations are then fetched together
-    const int tile = __ldg(&L.tiles[blockIdx.x]);
-    const uint32_t mask = __ldg(&L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)]);
-    const int tx = tile % L.tiles_x, ty = tile / L.tiles_x;
+    // the tile id and this row's plain-cell mask are independent loads
+    const int tile = __ldg(&L.tiles[t]); // tx | ty << 16
+    const uint32_t mask = __ldg(&L.tile_mask[t * 8 + (threadIdx.x >> 5)]);
+    const int tx = tile & 0xFFFF, ty = tile >> 16;
     const int x = tx * 32 + (threadIdx.x & 31);
     const int y = ty * 8 + (threadIdx.x >> 5);
     // tiles off the border reach their neighbours without wrapping
     const bool interior = tx > 0 && tx + 1 < L.tiles_x && ty > 0 && ty + 1 < (L.H + 7) / 8;
-    double r_diff = 0.0, r_norm = 0.0;
     if ((mask >> (threadIdx.x & 31)) & 1u)
     {
         const int64_t s = site_of(L, x, y);
+        // (a "direct" state is read like an even step: own slots)
         float df[9];
-        if (o.direct) load_raw_ro<0>(L, x, y, df);
-        else load_raw_ro<P>(L, x, y, df, interior);
+        load_raw_ro<P>(L, x, y, df, interior);
         const float om = __ldg(&L.omega[s]);
         SpecialRec none;
-        step_cell<P>(L, C, o, x, y, s, df, om, false, none, r_diff, r_norm, interior);
+        step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior);
     }
-    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 
-// Persistent, software-pipelined variant of k_plain: each block walks the
-// tiles blockIdx.x, blockIdx.x + gridDim.x, ... and issues the loads of its
-// next tile before colliding and storing the current one, so that memory
-// requests stay in flight during the arithmetic.  The next tile's slots are
-// disjoint from the current tile's (AA ownership), so the early loads are safe.
-template <int P> __global__ void __launch_bounds__(256, 4) k_plain_pipe(LevelView L, Common C, StepOpt o)
-{
-    double r_diff = 0.0, r_norm = 0.0;
-    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    int t = blockIdx.x;
-    float cur[9], nxt[9];
-    float ctau = 0.0f;
-    int cx = 0, cy = 0;
-    auto fetch = [&](int tile, float v[9], float &tau, int &x, int &y) {
-        const int tt = __ldg(&L.tiles[tile]);
-        x = (tt % L.tiles_x) * 32 + lx;
-        y = (tt / L.tiles_x) * 8 + ly;
-        tau = 0.0f;
-        if (x < L.W && y < L.H)
-        {
-            tau = __ldg(&L.omega[site_of(L, x, y)]);
-            if (tau > 0.0f)
-            {
-                if (o.direct) load_raw_ro<0>(L, x, y, v);
-                else load_raw_ro<P>(L, x, y, v);
-            }
-        }
-    };
-    if (t < L.ntiles) fetch(t, cur, ctau, cx, cy);
-    for (; t < L.ntiles; t += gridDim.x)
-    {
-        const int tn = t + gridDim.x;
-        float ntau = 0.0f;
-        int nx = 0, ny = 0;
-        if (tn < L.ntiles) fetch(tn, nxt, ntau, nx, ny);
-        if (ctau > 0.0f)
-        {
-            SpecialRec none;
-            double rd = 0.0, rn = 0.0;
-            step_cell<P>(L, C, o, cx, cy, site_of(L, cx, cy), cur, ctau, false, none, rd, rn);
-            r_diff += rd;
-            r_norm += rn;
-        }
-#pragma unroll
-        for (int q = 0; q < 9; q++) cur[q] = nxt[q];
-        ctau = ntau;
-        cx = nx;
-        cy = ny;
-    }
-    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
-}
-
-// Special cells of one level, from the level's site-sorted record range.
+// One special cell (wall links, missing arrivals, interface buffer, inlet /
+// outlet) from its record.
 template <int P>
-__global__ void __launch_bounds__(128) k_special(LevelView L, Common C, StepOpt o, int64_t begin, int count)
+__device__ __forceinline__ void special_cell(const LevelView &L, const Common &C, const StepOpt &o, int64_t i, int diff,
+                                             int store_u, double &r_diff, double &r_norm)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double r_diff = 0.0, r_norm = 0.0;
-    if (i < count)
+    const SpecialRec rec = C.specials[i];
+    const int x = rec.site % L.pitch, y = rec.site / L.pitch;
+    float df[9];
+    const uint32_t flags = (rec.m1 >> 17) & 0xFu;
+    if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
     {
-        const SpecialRec rec = C.specials[begin + i];
-        const int x = rec.site % L.pitch, y = rec.site / L.pitch;
-        float df[9];
-        const uint32_t flags = (rec.m1 >> 17) & 0xFu;
-        if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
-        {
 #pragma unroll
-            for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + rec.buf];
-        }
-        else if (o.direct)
-            load_raw<0>(L, x, y, df);
-        else
-            load_special<P>(L, C, rec, x, y, df);
-        step_cell<P>(L, C, o, x, y, (int64_t)rec.site, df, rec.omega, true, rec, r_diff, r_norm);
+        for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + rec.buf];
     }
-    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+    else if (o.direct)
+        load_raw<0>(L, x, y, df);
+    else
+        load_special<P>(L, C, rec, x, y, df);
+    step_cell<P>(L, C, o, diff, store_u, x, y, (int64_t)rec.site, df, rec.omega, true, rec, r_diff, r_norm);
+}
+
+// ---- phase kernels.  A coarse time step is a sequence of phases; a phase
+// steps every (image, level) whose next substep falls on it.  All levels of an
+// image are independent within a coarse step (they meet only in the interface
+// exchange that closes it), so one launch covers them all.  The descriptors
+// travel in the launch parameters: each owns a contiguous block range, so the
+// descriptor index and its fields are block-uniform.
+
+// One (image, level) in one phase: where its state is and how to step it.
+struct StepDesc
+{
+    LevelView L;
+    Common C;
+    StepOpt o;
+    int64_t spec_begin; // the level's special records
+    int spec_count;
+    int pad_;
+};
+
+// Per-launch residual switches: the residual terms (and the |u| store) apply
+// to the first substep of each level, which falls on phase 0.
+struct PhaseArgs
+{
+    int diff, store_u, red_slot;
+};
+
+constexpr int kMaxPhaseDescs = 24;
+
+struct PhaseLaunch
+{
+    int ndesc;
+    int start[kMaxPhaseDescs + 1]; // first block of each descriptor; start[ndesc] = blocks
+    PhaseArgs a;
+    StepDesc d[kMaxPhaseDescs];
+};
+
+// descriptor owning block b (block-uniform)
+__device__ __forceinline__ int owner(const int *start, int n, int b)
+{
+    int j = 0;
+#pragma unroll 1
+    while (j + 1 < n && b >= start[j + 1]) j++;
+    return j;
+}
+
+// plain cells: blocks of a descriptor walk its active tiles
+__global__ void __launch_bounds__(256, 6) k_phase_plain(const __grid_constant__ PhaseLaunch P)
+{
+    const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
+    const StepDesc &d = P.d[j];
+    const int t = (int)blockIdx.x - P.start[j];
+    const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
+    double r_diff = 0.0, r_norm = 0.0;
+    if (d.o.parity) plain_tile<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+    else plain_tile<0>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+    if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
+}
+
+// special cells: blocks of a descriptor walk its records, 128 per block
+__global__ void __launch_bounds__(128) k_phase_special(const __grid_constant__ PhaseLaunch P)
+{
+    const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
+    const StepDesc &d = P.d[j];
+    const int i = ((int)blockIdx.x - P.start[j]) * 128 + (int)threadIdx.x;
+    const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
+    double r_diff = 0.0, r_norm = 0.0;
+    if (i < d.spec_count)
+    {
+        if (d.o.parity) special_cell<1>(d.L, d.C, d.o, d.spec_begin + i, diff, store_u, r_diff, r_norm);
+        else special_cell<0>(d.L, d.C, d.o, d.spec_begin + i, diff, store_u, r_diff, r_norm);
+    }
+    if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
 }
 
 // Maximum of a non-negative double over the block, then one atomic per block
@@ -304,9 +321,9 @@ __device__ __forceinline__ void block_max(double v, double *dst)
 // since the previous step (maximum over the cells).
 template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
 {
-    const int tile = L.tiles[blockIdx.x];
-    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
-    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
+    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
+    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
     double rmax = 0.0;
     if (x < L.W && y < L.H && L.omega[site_of(L, x, y)] != 0.0f)
     {
@@ -334,9 +351,9 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, C
 // applied when the populations are read in the next step.
 template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
 {
-    const int tile = L.tiles[blockIdx.x];
-    const int x = (tile % L.tiles_x) * 32 + (threadIdx.x & 31);
-    const int y = (tile / L.tiles_x) * 8 + (threadIdx.x >> 5);
+    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
+    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
+    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
     if (x >= L.W || y >= L.H) return;
     const int64_t s = site_of(L, x, y);
     if (L.omega[s] == 0.0f) return;
@@ -478,11 +495,9 @@ __global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int3
 // Coarse buffer cells <- rescaled mean of their 4 children
 // (include/coreLB.hpp:1104-1135): f_c = f_eq,c + 2 tau_c / mean(tau_f) (mean(f_f) - f_eq,c).
 template <int PF>
-__global__ void __launch_bounds__(128) k_coarse(LevelView Lf, LevelView Lc, Common C, const CoarseRowDev *rows, int nrows)
+__device__ __forceinline__ void coarse_row(const LevelView &Lf, const LevelView &Lc, const Common &C,
+                                           const CoarseRowDev &row)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nrows) return;
-    const CoarseRowDev row = rows[r];
     float mean[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 4; k++)
     {
@@ -514,11 +529,8 @@ __global__ void __launch_bounds__(128) k_coarse(LevelView Lf, LevelView Lc, Comm
 // (include/coreLB.hpp:1137-1230); the spline is linear in the node values, so
 // each child holds 6 precomputed weights.  f = f_eq + tau_f / (2 tau_c) (f_spline - f_eq).
 template <int PC>
-__global__ void __launch_bounds__(128) k_fine(LevelView Lf, LevelView Lc, Common C, const FineRowDev *rows, int nrows)
+__device__ __forceinline__ void fine_row(const LevelView &Lf, const LevelView &Lc, const Common &C, const FineRowDev &row)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nrows) return;
-    const FineRowDev &row = rows[r];
     float z[6][9];
     for (int k = 0; k < 6; k++)
     {
@@ -549,6 +561,50 @@ __global__ void __launch_bounds__(128) k_fine(LevelView Lf, LevelView Lc, Common
             for (int k = 0; k < 6; k++) v += row.weight[c][k] * z[k][q];
             C.ibuf[(size_t)q * C.n_buf + row.child_buf[c]] = feq[q] + rat * (v - feq[q]);
         }
+    }
+}
+
+// One level pair of one image in the interface exchange: the two levels'
+// states (at their parities after the coarse step) and the pair's rows.
+struct PairDesc
+{
+    LevelView Lf, Lc;
+    Common C;
+    const CoarseRowDev *coarse;
+    const FineRowDev *fine;
+    int pf, pc;  // parity of the next step of the fine / coarse level
+    int kind;    // rows of this entry: 0 coarse, 1 fine
+    int nrows;
+};
+
+constexpr int kMaxWaveDescs = 16;
+
+struct WaveLaunch
+{
+    int ndesc;
+    int start[kMaxWaveDescs + 1];
+    PairDesc d[kMaxWaveDescs];
+};
+
+// Interface exchange wave: coarse rows of some pairs and fine rows of others
+// (independent within a wave), 128 rows per block.
+__global__ void __launch_bounds__(128) k_wave(const __grid_constant__ WaveLaunch W)
+{
+    const int j = owner(W.start, W.ndesc, (int)blockIdx.x);
+    const PairDesc &d = W.d[j];
+    const int r = ((int)blockIdx.x - W.start[j]) * 128 + (int)threadIdx.x;
+    if (r >= d.nrows) return;
+    if (d.kind == 0)
+    {
+        const CoarseRowDev row = d.coarse[r];
+        if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row);
+        else coarse_row<0>(d.Lf, d.Lc, d.C, row);
+    }
+    else
+    {
+        const FineRowDev &row = d.fine[r];
+        if (d.pc) fine_row<1>(d.Lf, d.Lc, d.C, row);
+        else fine_row<0>(d.Lf, d.Lc, d.C, row);
     }
 }
 

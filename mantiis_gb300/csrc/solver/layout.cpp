@@ -293,7 +293,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
                             break;
                         }
                 if (!any) continue;
-                lv.tile_list.push_back(ty * lv.tiles_x + tx);
+                lv.tile_list.push_back(tx | ty << 16);
                 for (int r = 0; r < 8; r++)
                 {
                     uint32_t m = 0;

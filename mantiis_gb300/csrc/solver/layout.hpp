@@ -70,7 +70,7 @@ struct LevelLayout
     std::vector<float> omega;        // per site 1/tau_s: 0 inactive, >0 plain, <0 special
     std::vector<float> tau_d;        // per site tau_d of the plain MRT (adsorption), else empty
     std::vector<uint32_t> spec;      // per site: special record index (valid when tau < 0)
-    std::vector<int32_t> tile_list;  // active 32x8 tiles: ty * tiles_x + tx
+    std::vector<int32_t> tile_list;  // active 32x8 tiles: tx | ty << 16
     std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
     int tiles_x = 0, tiles_y = 0;
     int64_t n_active = 0, n_active_real = 0;

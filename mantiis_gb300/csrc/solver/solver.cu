@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <random>
@@ -114,6 +115,27 @@ struct InterfaceDev
 
 constexpr int kRing = 8192; // residual accumulator slots (4 doubles each)
 
+// Launch parameters of one state of the step parities over a group of
+// images: per phase the plain- and special-cell launches (each with up to
+// kMaxPhaseDescs level descriptors), per interface wave its launches.
+struct PhaseVariant
+{
+    std::vector<std::vector<dev::PhaseLaunch>> plain, spec; // per phase
+    std::vector<std::vector<dev::WaveLaunch>> waves;        // per wave
+};
+
+// Phase schedule of a group of images: which (image, level, substep) each
+// phase steps, and the level pairs of the interface exchange.
+struct PhasePlan
+{
+    int nphase = 1, nwave = 0;
+    // per phase: (image, level - 1, substep k, steps the level has taken in
+    // this coarse step before this phase)
+    std::vector<std::vector<int4>> entries;
+    std::vector<int2> pairs; // (image, interface index)
+    std::map<std::string, PhaseVariant> variants;
+};
+
 } // namespace
 
 struct mgpu_ctx
@@ -143,8 +165,10 @@ struct mgpu_ctx
     bool adsorption = false; // Shan-Chen step body (include/mantiisApp.hpp:248-265)
 
     cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
+    std::string graph_key;           // level parities the graph was captured at
     int64_t graph_launches = 0;
-    int plain_variant = 0;          // 0: one block per tile, 1: persistent pipelined
+    std::unique_ptr<PhasePlan> plan; // phase engine tables of this image
+    std::vector<std::unique_ptr<PhasePlan>> level_plans; // single-level tables (mgpu_step_level)
     int sm_count = 1;
     int64_t coarse_done = 0;     // coarse steps executed since creation
     int64_t ref_t = 0;           // reference lb->t
@@ -292,49 +316,21 @@ void launch_check(mgpu_ctx *ctx)
     CK(cudaGetLastError());
 }
 
-// the two kernels of one substep of one level: plain cells over the active
-// tiles, special cells over the level's record range (disjoint slot sets)
-void launch_level(mgpu_ctx *ctx, int l, const dev::LevelView &V, const dev::Common &C, const dev::StepOpt &o)
-{
-    const LevelLayout &ll = ctx->lay.levels[l];
-    // fork: the special-cell kernel runs beside the plain-cell kernel (their
-    // slot sets are disjoint under the AA ownership rule)
-    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
-    if (!ll.tile_list.empty())
-    {
-        if (ctx->plain_variant == 1)
-        {
-            int blocks = std::min((int)ll.tile_list.size(), ctx->sm_count * 4);
-            dim3 grid((unsigned)blocks), block(256);
-            if (o.parity == 0) dev::k_plain_pipe<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_plain_pipe<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
-        }
-        else
-        {
-            dim3 grid((unsigned)ll.tile_list.size()), block(256);
-            if (o.parity == 0) dev::k_plain<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_plain<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
-        }
-        launch_check(ctx);
-    }
-    if (ll.spec_count)
-    {
-        int n = (int)ll.spec_count;
-        dim3 grid((unsigned)((n + 127) / 128)), block(128);
-        if (o.parity == 0) dev::k_special<0><<<grid, block, 0, ctx->side_stream>>>(V, C, o, ll.spec_begin, n);
-        else dev::k_special<1><<<grid, block, 0, ctx->side_stream>>>(V, C, o, ll.spec_begin, n);
-        launch_check(ctx);
-    }
-    // join: the next kernel on the main stream waits for the special cells
-    CK(cudaEventRecord(ctx->ev_join, ctx->side_stream));
-    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-}
+// ---- phase engine, host side.  Substep k of level l (0-based) of an image
+// with L levels, in a group whose deepest image has Lmax levels, falls on
+// phase k * 2^(Lmax - L + l): every level's first substep on phase 0.
+std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int only_level);
+std::string state_key(const std::vector<mgpu_ctx *> &ctxs, int ahead);
+PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, int ahead);
+void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::PhaseLaunch> &spec,
+                  const dev::PhaseArgs &a, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                  int64_t &launches);
+void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, cudaStream_t side,
+                cudaEvent_t fork, cudaEvent_t join, dev::PhaseArgs a, int64_t &launches);
 
 // ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
 void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
 {
-    const int L = ctx->lay.max_level;
     dev::Common C = ctx->common();
     if (ctx->adsorption)
     {
@@ -362,62 +358,18 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         ctx->coarse_done++;
         return;
     }
-    const bool mb = ctx->grid.multiblock;
-    for (int l = L - 1; l >= 0; l--)
-    {
-        LevelLayout &ll = ctx->lay.levels[l];
-        if (ll.tile_list.empty())
-        {
-            ctx->lv[l].steps += ll.substeps;
-            continue;
-        }
-        for (int sub = 0; sub < ll.substeps; sub++)
-        {
-            dev::LevelView V = ctx->view(l);
-            dev::StepOpt o{};
-            o.parity = (int)(ctx->lv[l].steps & 1);
-            o.direct = ctx->lv[l].steps == 0 ? 1 : 0;
-            o.first_sub = sub == 0;
-            o.snap_store = mb && sub == 0;
-            o.snap_use = mb && sub > 0;
-            o.diff = (sub == 0 && diff) ? 1 : 0;
-            o.store_u = (sub == 0 && store_u) ? 1 : 0;
-            o.red_slot = red_slot;
-            launch_level(ctx, l, V, C, o);
-            ctx->lv[l].steps++;
-        }
-    }
-    // interface exchange, finest first (include/coreLB.hpp:1327-1330)
-    for (auto &it : ctx->itf)
-    {
-        int l1 = it.l1 - 1, l2 = it.l1;
-        dev::LevelView Vf = ctx->view(l1), Vc = ctx->view(l2);
-        int pf = (int)(ctx->lv[l1].steps & 1), pc = (int)(ctx->lv[l2].steps & 1);
-        if (it.ncoarse)
-        {
-            dim3 grid((it.ncoarse + 127) / 128), block(128);
-            if (pf == 0) dev::k_coarse<0><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.coarse.p, it.ncoarse);
-            else dev::k_coarse<1><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.coarse.p, it.ncoarse);
-            launch_check(ctx);
-        }
-        if (it.nfine)
-        {
-            dim3 grid((it.nfine + 127) / 128), block(128);
-            if (pc == 0) dev::k_fine<0><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.fine.p, it.nfine);
-            else dev::k_fine<1><<<grid, block, 0, ctx->stream>>>(Vf, Vc, C, it.fine.p, it.nfine);
-            launch_check(ctx);
-        }
-    }
-    ctx->coarse_done++;
+    dev::PhaseArgs a{diff ? 1 : 0, store_u ? 1 : 0, red_slot};
+    phase_step(*ctx->plan, {ctx}, ctx->stream, ctx->side_stream, ctx->ev_fork, ctx->ev_join, a, ctx->launches);
 }
 
 // read pass over all reference cells
-void cells_pass(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f, bool diff, bool store_u, int red_slot)
+void cells_pass(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f, bool diff, bool store_u, int red_slot,
+                cudaStream_t st = nullptr)
 {
     int64_t n = ctx->grid.n_cells;
     if (n == 0) return;
     dim3 grid((unsigned)((n + 255) / 256)), block(256);
-    dev::k_cells<<<grid, block, 0, ctx->stream>>>(ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, rho,
+    dev::k_cells<<<grid, block, 0, st ? st : ctx->stream>>>(ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, rho,
                                                    ux, uy, f, diff ? 1 : 0, store_u ? 1 : 0, red_slot);
     launch_check(ctx);
 }
@@ -525,6 +477,217 @@ double residual_of(const mgpu_ctx *ctx, const double *v)
     return v[0] / v[1];
 }
 
+std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int only_level)
+{
+    std::unique_ptr<PhasePlan> P(new PhasePlan());
+    int Lmax = 1;
+    for (auto *c : ctxs) Lmax = std::max(Lmax, c->lay.max_level);
+    P->nphase = only_level >= 0 ? 1 : 1 << (Lmax - 1);
+    P->entries.resize(P->nphase);
+    for (int ph = 0; ph < P->nphase; ph++)
+        for (size_t i = 0; i < ctxs.size(); i++)
+        {
+            const ImageLayout &lay = ctxs[i]->lay;
+            const int L = lay.max_level;
+            for (int l = 0; l < L; l++)
+            {
+                const LevelLayout &ll = lay.levels[l];
+                if (ll.tile_list.empty() && ll.spec_count == 0) continue;
+                if (only_level >= 0)
+                {
+                    // flags of a middle substep (snapshot in use, no buffer refresh)
+                    if (l == only_level) P->entries[ph].push_back(make_int4((int)i, l, 1, 0));
+                    continue;
+                }
+                const int stride = 1 << (Lmax - L + l);
+                if (ph % stride) continue;
+                P->entries[ph].push_back(make_int4((int)i, l, ph / stride, ph / stride));
+            }
+        }
+    if (only_level >= 0) return P;
+    // interface waves (include/coreLB.hpp:1327-1330 runs pairs (1,2), (2,3), ...
+    // each coarse rows first): coarse rows of pair (l, l+1) read level-l cells
+    // and buffers refreshed by the coarse rows of (l-1, l); fine rows of (l, l+1)
+    // read level-(l+1) cells and buffers refreshed by the coarse rows of (l, l+1).
+    // So wave w = coarse rows of pair (w+1, w+2) and fine rows of pair (w, w+1).
+    P->nwave = Lmax >= 2 ? Lmax : 0;
+    for (size_t i = 0; i < ctxs.size(); i++)
+        for (int p = 0; p < (int)ctxs[i]->itf.size(); p++) P->pairs.push_back(make_int2((int)i, p));
+    return P;
+}
+
+// parity and "never stepped" state of every level, `ahead` coarse steps on
+std::string state_key(const std::vector<mgpu_ctx *> &ctxs, int ahead)
+{
+    std::string key;
+    for (auto *c : ctxs)
+        for (size_t l = 0; l < c->lv.size(); l++)
+        {
+            const int64_t st = c->lv[l].steps + (int64_t)ahead * c->lay.levels[l].substeps;
+            key.push_back((char)('0' + (int)(st & 1) + (st == 0 ? 2 : 0)));
+        }
+    return key;
+}
+
+// splits a list of descriptors with their block counts into launches
+template <typename Launch, typename Desc, int Max>
+std::vector<Launch> pack_launches(const std::vector<std::pair<Desc, int>> &items)
+{
+    std::vector<Launch> out;
+    for (size_t i = 0; i < items.size(); i += Max)
+    {
+        Launch l;
+        std::memset(&l, 0, sizeof(l));
+        const int n = (int)std::min<size_t>(Max, items.size() - i);
+        l.ndesc = n;
+        int blocks = 0;
+        for (int j = 0; j < n; j++)
+        {
+            l.start[j] = blocks;
+            l.d[j] = items[i + j].first;
+            blocks += items[i + j].second;
+        }
+        l.start[n] = blocks;
+        out.push_back(l);
+    }
+    return out;
+}
+
+// Launch parameters for the state `ahead` coarse steps after the current one.
+PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, int ahead)
+{
+    const std::string key = state_key(ctxs, ahead);
+    auto found = P.variants.find(key);
+    if (found != P.variants.end()) return found->second;
+    auto steps_of = [&](const mgpu_ctx *c, int l) {
+        return c->lv[l].steps + (int64_t)ahead * c->lay.levels[l].substeps;
+    };
+    PhaseVariant V;
+    V.plain.resize(P.nphase);
+    V.spec.resize(P.nphase);
+    for (int ph = 0; ph < P.nphase; ph++)
+    {
+        std::vector<std::pair<dev::StepDesc, int>> pl, sp;
+        for (const int4 &e : P.entries[ph])
+        {
+            const mgpu_ctx *c = ctxs[e.x];
+            const int l = e.y, k = e.z;
+            const LevelLayout &ll = c->lay.levels[l];
+            const int64_t st = steps_of(c, l) + e.w;
+            const bool mb = c->grid.multiblock;
+            dev::StepDesc sd;
+            std::memset(&sd, 0, sizeof(sd));
+            sd.L = c->view(l);
+            sd.C = c->common();
+            sd.o.parity = (int)(st & 1);
+            sd.o.direct = st == 0 ? 1 : 0;
+            sd.o.first_sub = k == 0 ? 1 : 0;
+            sd.o.snap_store = (mb && k == 0) ? 1 : 0;
+            sd.o.snap_use = (mb && k > 0) ? 1 : 0;
+            sd.spec_begin = ll.spec_begin;
+            sd.spec_count = (int)ll.spec_count;
+            if (!ll.tile_list.empty()) pl.push_back({sd, (int)ll.tile_list.size()});
+            if (ll.spec_count) sp.push_back({sd, (int)((ll.spec_count + 127) / 128)});
+        }
+        V.plain[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(pl);
+        V.spec[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(sp);
+    }
+    std::vector<std::vector<std::pair<dev::PairDesc, int>>> wv(P.nwave);
+    for (const int2 &pr : P.pairs)
+    {
+        const mgpu_ctx *c = ctxs[pr.x];
+        const InterfaceDev &it = c->itf[pr.y];
+        const int lf = it.l1 - 1, lc = it.l1;
+        dev::PairDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.Lf = c->view(lf);
+        d.Lc = c->view(lc);
+        d.C = c->common();
+        d.coarse = it.coarse.p;
+        d.fine = it.fine.p;
+        // parities once the level has taken this coarse step's substeps
+        d.pf = (int)((steps_of(c, lf) + c->lay.levels[lf].substeps) & 1);
+        d.pc = (int)((steps_of(c, lc) + c->lay.levels[lc].substeps) & 1);
+        if (it.ncoarse)
+        {
+            d.kind = 0;
+            d.nrows = it.ncoarse;
+            wv[it.l1 - 1].push_back({d, (it.ncoarse + 127) / 128});
+        }
+        if (it.nfine)
+        {
+            d.kind = 1;
+            d.nrows = it.nfine;
+            wv[it.l1].push_back({d, (it.nfine + 127) / 128});
+        }
+    }
+    V.waves.resize(P.nwave);
+    for (int w = 0; w < P.nwave; w++) V.waves[w] = pack_launches<dev::WaveLaunch, dev::PairDesc, dev::kMaxWaveDescs>(wv[w]);
+    return P.variants.emplace(key, std::move(V)).first->second;
+}
+
+// The launches of one phase: plain-cell blocks on `main`, special-cell blocks
+// forked onto `side` (their slot sets are disjoint under the AA ownership rule).
+void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::PhaseLaunch> &spec,
+                  const dev::PhaseArgs &a, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                  int64_t &launches)
+{
+    const bool both = !plain.empty() && !spec.empty();
+    if (both)
+    {
+        CK(cudaEventRecord(fork, main));
+        CK(cudaStreamWaitEvent(side, fork, 0));
+    }
+    for (const auto &l0 : plain)
+    {
+        dev::PhaseLaunch l = l0;
+        l.a = a;
+        dev::k_phase_plain<<<(unsigned)l.start[l.ndesc], 256, 0, main>>>(l);
+        CK(cudaGetLastError());
+        launches++;
+    }
+    for (const auto &l0 : spec)
+    {
+        dev::PhaseLaunch l = l0;
+        l.a = a;
+        dev::k_phase_special<<<(unsigned)l.start[l.ndesc], 128, 0, both ? side : main>>>(l);
+        CK(cudaGetLastError());
+        launches++;
+    }
+    if (both)
+    {
+        CK(cudaEventRecord(join, side));
+        CK(cudaStreamWaitEvent(main, join, 0));
+    }
+}
+
+// One coarse step of every image of the group: the phases, then the
+// interface waves.
+void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, cudaStream_t side,
+                cudaEvent_t fork, cudaEvent_t join, dev::PhaseArgs a, int64_t &launches)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(main, &cs));
+    if (cs != cudaStreamCaptureStatusNone && !P.variants.count(state_key(ctxs, 0)))
+        throw std::logic_error("phase launches missing during graph capture");
+    PhaseVariant &V = plan_variant(P, ctxs, 0);
+    const dev::PhaseArgs none{0, 0, 0};
+    for (int ph = 0; ph < P.nphase; ph++)
+        launch_phase(V.plain[ph], V.spec[ph], ph == 0 ? a : none, main, side, fork, join, launches);
+    for (int w = 0; w < P.nwave; w++)
+        for (const auto &l : V.waves[w])
+        {
+            dev::k_wave<<<(unsigned)l.start[l.ndesc], 128, 0, main>>>(l);
+            CK(cudaGetLastError());
+            launches++;
+        }
+    for (auto *c : ctxs)
+    {
+        for (size_t l = 0; l < c->lv.size(); l++) c->lv[l].steps += c->lay.levels[l].substeps;
+        c->coarse_done++;
+    }
+}
+
 void check_supported(mgpu_ctx *ctx)
 {
     if (ctx->prm.simulation == MGPU_SIM_COUPLED)
@@ -607,7 +770,6 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
 
     CK(cudaGetDevice(&ctx->device));
     CK(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device));
-    if (const char *v = std::getenv("MGPU_PLAIN_VARIANT")) ctx->plain_variant = std::atoi(v);
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
     CK(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
@@ -665,6 +827,8 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         e.coarse.upload(it.coarse, acct, s);
         e.fine.upload(it.fine, acct, s);
     }
+
+    if (!ctx->adsorption) ctx->plan = build_plan({ctx.get()}, -1);
 
     // initial state: rho = rho_init, u = 0, f = f_eq (include/coreLB.hpp:381-417)
     std::vector<double> rho(ctx->grid.n_cells, rho_init), zero(ctx->grid.n_cells, 0.0);
@@ -856,9 +1020,21 @@ int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
             coarse_step(ctx, false, false, 0);
             left--;
         }
+        if (left >= 2 && ctx->graph && ctx->graph_key != state_key({ctx}, 0))
+        {
+            // captured at other step parities
+            CK(cudaGraphExecDestroy(ctx->graph));
+            ctx->graph = nullptr;
+        }
         if (left >= 2 && !ctx->graph)
         {
+            ctx->graph_key = state_key({ctx}, 0);
             // capture two coarse steps: every level then returns to its parity
+            if (ctx->plan)
+            {
+                plan_variant(*ctx->plan, {ctx}, 0);
+                plan_variant(*ctx->plan, {ctx}, 1);
+            }
             std::vector<int64_t> saved;
             for (auto &l : ctx->lv) saved.push_back(l.steps);
             int64_t saved_done = ctx->coarse_done, saved_launch = ctx->launches;
@@ -892,18 +1068,17 @@ int mgpu_step_level(mgpu_ctx *ctx, int level, int n)
 {
     return guarded(ctx, [&]() {
         if (!ctx || level < 1 || level > (int)ctx->lv.size() || n < 0) throw std::invalid_argument("bad argument");
-        int l = level - 1;
-        const LevelLayout &ll = ctx->lay.levels[l];
-        if (ll.tile_list.empty()) return MGPU_OK;
-        dev::Common C = ctx->common();
+        if (ctx->adsorption) throw std::logic_error("mgpu_step_level steps the transport kernels");
+        const int l = level - 1;
+        if ((int)ctx->level_plans.size() < level) ctx->level_plans.resize(level);
+        if (!ctx->level_plans[l]) ctx->level_plans[l] = build_plan({ctx}, l);
+        PhasePlan &P = *ctx->level_plans[l];
+        const dev::PhaseArgs none{0, 0, 0};
         for (int i = 0; i < n; i++)
         {
-            dev::StepOpt o{};
-            o.parity = (int)(ctx->lv[l].steps & 1);
-            o.direct = ctx->lv[l].steps == 0 ? 1 : 0;
-            o.snap_use = ctx->grid.multiblock ? 1 : 0;
-            dev::LevelView V = ctx->view(l);
-            launch_level(ctx, l, V, C, o);
+            PhaseVariant &V = plan_variant(P, {ctx}, 0);
+            launch_phase(V.plain[0], V.spec[0], none, ctx->stream, ctx->side_stream, ctx->ev_fork, ctx->ev_join,
+                         ctx->launches);
             ctx->lv[l].steps++;
         }
         return MGPU_OK;
@@ -1142,6 +1317,236 @@ int mgpu_set_stream(mgpu_ctx *ctx, void *stream)
 }
 
 int64_t mgpu_launch_count(const mgpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+} // extern "C"
+
+// A group of transport contexts stepped together: each phase of a coarse step
+// is one launch over all images, each interface wave one launch.
+struct mgpu_batch
+{
+    std::vector<mgpu_ctx *> ctxs;
+    std::unique_ptr<PhasePlan> plan;
+    cudaStream_t stream = nullptr, side = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
+    std::vector<cudaEvent_t> ctx_ev;
+    cudaGraphExec_t graph = nullptr;
+    std::string graph_key;
+    int64_t graph_launches = 0, launches = 0;
+};
+
+namespace
+{
+// the batch's work starts after each context's earlier work ...
+void batch_enter(mgpu_batch *b)
+{
+    for (size_t i = 0; i < b->ctxs.size(); i++)
+        if (b->ctxs[i]->stream != b->stream)
+        {
+            CK(cudaEventRecord(b->ctx_ev[i], b->ctxs[i]->stream));
+            CK(cudaStreamWaitEvent(b->stream, b->ctx_ev[i], 0));
+        }
+}
+// ... and each context's later work starts after the batch's
+void batch_leave(mgpu_batch *b)
+{
+    CK(cudaEventRecord(b->ev_done, b->stream));
+    for (auto *c : b->ctxs)
+        if (c->stream != b->stream) CK(cudaStreamWaitEvent(c->stream, b->ev_done, 0));
+}
+
+void batch_step(mgpu_batch *b)
+{
+    phase_step(*b->plan, b->ctxs, b->stream, b->side, b->ev_fork, b->ev_join, dev::PhaseArgs{0, 0, 0}, b->launches);
+    for (auto *c : b->ctxs) c->ref_t++;
+}
+} // namespace
+
+extern "C" {
+
+int mgpu_batch_create(mgpu_ctx *const *ctxs, int n, mgpu_batch **out)
+{
+    return guarded(nullptr, [&]() {
+        if (!ctxs || n <= 0 || !out) throw std::invalid_argument("bad argument");
+        std::unique_ptr<mgpu_batch> b(new mgpu_batch());
+        int dev = -1;
+        CK(cudaGetDevice(&dev));
+        for (int i = 0; i < n; i++)
+        {
+            mgpu_ctx *c = ctxs[i];
+            if (!c) throw std::invalid_argument("null context in batch");
+            if (c->adsorption || !c->plan) throw std::invalid_argument("a batch steps transport contexts only");
+            if (c->device != dev) throw std::invalid_argument("batch contexts must live on the current device");
+            for (int k = 0; k < i; k++)
+                if (ctxs[k] == c) throw std::invalid_argument("context listed twice in batch");
+            b->ctxs.push_back(c);
+        }
+        b->plan = build_plan(b->ctxs, -1);
+        CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        b->own_stream = true;
+        CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
+        b->ctx_ev.resize(b->ctxs.size());
+        for (auto &e : b->ctx_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        *out = b.release();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_advance(mgpu_batch *b, int n_steps)
+{
+    return guarded(nullptr, [&]() {
+        if (!b || n_steps < 0) throw std::invalid_argument("bad argument");
+        batch_enter(b);
+        int left = n_steps;
+        // the graph starts from a stepped state (not the initial "direct" one)
+        bool fresh = false;
+        for (auto *c : b->ctxs)
+            for (auto &l : c->lv) fresh |= l.steps == 0;
+        if (fresh && left > 0)
+        {
+            batch_step(b);
+            left--;
+        }
+        if (left >= 2 && b->graph && b->graph_key != state_key(b->ctxs, 0))
+        {
+            CK(cudaGraphExecDestroy(b->graph));
+            b->graph = nullptr;
+        }
+        if (left >= 2 && !b->graph)
+        {
+            // two coarse steps: every level of every image returns to its parity
+            plan_variant(*b->plan, b->ctxs, 0);
+            plan_variant(*b->plan, b->ctxs, 1);
+            b->graph_key = state_key(b->ctxs, 0);
+            std::vector<std::vector<int64_t>> saved;
+            std::vector<int64_t> saved_done, saved_t;
+            for (auto *c : b->ctxs)
+            {
+                saved.emplace_back();
+                for (auto &l : c->lv) saved.back().push_back(l.steps);
+                saved_done.push_back(c->coarse_done);
+                saved_t.push_back(c->ref_t);
+            }
+            const int64_t l0 = b->launches;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            batch_step(b);
+            batch_step(b);
+            CK(cudaStreamEndCapture(b->stream, &g));
+            CK(cudaGraphInstantiate(&b->graph, g, 0));
+            CK(cudaGraphDestroy(g));
+            b->graph_launches = b->launches - l0;
+            b->launches = l0;
+            for (size_t i = 0; i < b->ctxs.size(); i++)
+            {
+                for (size_t l = 0; l < b->ctxs[i]->lv.size(); l++) b->ctxs[i]->lv[l].steps = saved[i][l];
+                b->ctxs[i]->coarse_done = saved_done[i];
+                b->ctxs[i]->ref_t = saved_t[i];
+            }
+        }
+        while (left >= 2)
+        {
+            CK(cudaGraphLaunch(b->graph, b->stream));
+            for (auto *c : b->ctxs)
+            {
+                for (size_t l = 0; l < c->lv.size(); l++) c->lv[l].steps += 2 * c->lay.levels[l].substeps;
+                c->coarse_done += 2;
+                c->ref_t += 2;
+            }
+            b->launches += b->graph_launches;
+            left -= 2;
+        }
+        if (left == 1) batch_step(b);
+        batch_leave(b);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_observables(mgpu_batch *b, double *out)
+{
+    return guarded(nullptr, [&]() {
+        if (!b || !out) throw std::invalid_argument("null argument");
+        batch_enter(b);
+        const int slot = kRing - 1;
+        std::vector<double> v(4 * b->ctxs.size());
+        for (size_t i = 0; i < b->ctxs.size(); i++)
+        {
+            mgpu_ctx *c = b->ctxs[i];
+            CK(cudaMemsetAsync(c->red.p + (size_t)slot * 4, 0, 4 * sizeof(double), b->stream));
+            cells_pass(c, nullptr, nullptr, nullptr, nullptr, false, false, slot * 4, b->stream);
+            CK(cudaMemcpyAsync(&v[4 * i], c->red.p + (size_t)slot * 4, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                               b->stream));
+        }
+        CK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < b->ctxs.size(); i++)
+        {
+            const mgpu_ctx *c = b->ctxs[i];
+            const double npix = (double)c->grid.n * c->grid.n;
+            const double mean_ux = v[4 * i + 2] / npix;
+            const double nu = (c->lay.tau_mean - 0.5) / 3.0;
+            out[4 * i + 0] = mean_ux;
+            out[4 * i + 1] = c->prm.fbody != 0 ? mean_ux * nu / c->prm.fbody : 0.0;
+            out[4 * i + 2] = v[4 * i + 3];
+            out[4 * i + 3] = c->residuals.empty() ? 1.0 : c->residuals.back();
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_stream(mgpu_batch *b, void *stream)
+{
+    return guarded(nullptr, [&]() {
+        if (!b) throw std::invalid_argument("null batch");
+        CK(cudaStreamSynchronize(b->stream));
+        if (b->own_stream) CK(cudaStreamDestroy(b->stream));
+        if (b->graph)
+        {
+            CK(cudaGraphExecDestroy(b->graph));
+            b->graph = nullptr;
+        }
+        if (stream)
+        {
+            b->stream = (cudaStream_t)stream;
+            b->own_stream = false;
+        }
+        else
+        {
+            CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+            b->own_stream = true;
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_sync(mgpu_batch *b)
+{
+    return guarded(nullptr, [&]() {
+        if (!b) throw std::invalid_argument("null batch");
+        CK(cudaStreamSynchronize(b->stream));
+        return MGPU_OK;
+    });
+}
+
+int64_t mgpu_batch_launch_count(const mgpu_batch *b) { return b ? b->launches : 0; }
+
+int mgpu_batch_destroy(mgpu_batch *b)
+{
+    if (!b) return MGPU_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->side) cudaStreamSynchronize(b->side);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
+    for (auto e : b->ctx_ev) cudaEventDestroy(e);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return MGPU_OK;
+}
+
 
 const char *mgpu_last_error(const mgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
 const char *mgpu_global_error(void) { return g_error.c_str(); }

@@ -93,6 +93,13 @@ SIGNATURES = {
     "mgpu_set_equilibrium_noalloc": (C.c_int, [P, F64P, F64P, F64P]),
     "mgpu_set_stream": (C.c_int, [P, P]),
     "mgpu_launch_count": (C.c_int64, [P]),
+    "mgpu_batch_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
+    "mgpu_batch_advance": (C.c_int, [P, C.c_int]),
+    "mgpu_batch_observables": (C.c_int, [P, F64P]),
+    "mgpu_batch_set_stream": (C.c_int, [P, P]),
+    "mgpu_batch_sync": (C.c_int, [P]),
+    "mgpu_batch_launch_count": (C.c_int64, [P]),
+    "mgpu_batch_destroy": (C.c_int, [P]),
     "mgpu_last_error": (C.c_char_p, [P]),
     "mgpu_global_error": (C.c_char_p, []),
     "mgpu_grid_build": (C.c_int, [I32P, F64P, F64P, C.c_int, C.POINTER(Params), C.POINTER(P)]),
@@ -357,3 +364,53 @@ class Solver:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Several Solver contexts stepped together (include/mantiis_gpu.h, mgpu_batch):
+    one launch per phase over every image, two coarse steps per CUDA graph."""
+
+    def __init__(self, solvers):
+        self._h = None
+        self.solvers = list(solvers)
+        arr = (P * len(self.solvers))(*[s._h for s in self.solvers])
+        h = C.c_void_p()
+        rc = lib().mgpu_batch_create(arr, len(self.solvers), C.byref(h))
+        if rc != 0:
+            raise MantiisError(rc, lib().mgpu_global_error().decode())
+        self._h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MantiisError(rc, lib().mgpu_global_error().decode())
+
+    def advance(self, n_steps):
+        """Enqueues n coarse steps of every image; returns without waiting."""
+        self._check(lib().mgpu_batch_advance(self._h, int(n_steps)))
+
+    def observables(self):
+        out = np.zeros(4 * len(self.solvers))
+        self._check(lib().mgpu_batch_observables(self._h, out))
+        o = out.reshape(-1, 4)
+        return [dict(mean_ux=r[0], permeability=r[1], mass=r[2], residual=r[3]) for r in o]
+
+    def set_stream(self, stream_handle):
+        self._check(lib().mgpu_batch_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def sync(self):
+        self._check(lib().mgpu_batch_sync(self._h))
+
+    @property
+    def launches(self):
+        return int(lib().mgpu_batch_launch_count(self._h))
+
+    def close(self):
+        if self._h:
+            lib().mgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

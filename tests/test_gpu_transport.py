@@ -143,3 +143,30 @@ def test_deterministic(fixture64):
         s.advance(30)
         runs.append(s.cells(with_f=True)["f"])
     assert np.array_equal(runs[0], runs[1])
+
+
+def test_batch_matches_single_contexts(fixture64):
+    # a batch of images with 1, 2 and 3 levels steps each exactly like its own context
+    from mantiis_gb300 import Batch
+
+    imgs = [(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=1e-9))]
+    for n, levels, seed in ((128, 2, 11), (256, 3, 12)):
+        pore = generate_disks(n, 4 if n == 128 else 6, 10 if n == 128 else 30, 0.65, seed)
+        kn = np.where(pore == 1, 0.1, 0.0)
+        lp = np.where(pore == 1, 7.73, 0.0)
+        imgs.append((pore, kn, lp, default_params(multiblock=1, max_allowed_level=levels, edge_fine=1)))
+    solo = [Solver(*a) for a in imgs]
+    grouped = [Solver(*a) for a in imgs]
+    for s in solo:
+        s.advance(9)
+    b = Batch(grouped)
+    b.advance(4)   # the first step from the initial state, then a graph of two, then one
+    b.advance(5)
+    b.sync()
+    for s, g in zip(solo, grouped):
+        assert g.time == s.time
+        assert np.array_equal(s.cells(with_f=True)["f"], g.cells(with_f=True)["f"])
+    obs = b.observables()
+    for s, o in zip(solo, obs):
+        assert o["mean_ux"] == s.observables()["mean_ux"]
+    assert b.launches > 0
