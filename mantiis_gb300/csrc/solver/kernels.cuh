@@ -207,7 +207,7 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
                                              int store_u, double &r_diff, double &r_norm)
 {
     const SpecialRec rec = C.specials[i];
-    const int x = rec.site % L.pitch, y = rec.site / L.pitch;
+    const int x = rec.xy & 0xFFFF, y = rec.xy >> 16;
     float df[9];
     const uint32_t flags = (rec.m1 >> 17) & 0xFu;
     if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
@@ -219,7 +219,7 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
         load_raw<0>(L, x, y, df);
     else
         load_special<P>(L, C, rec, x, y, df);
-    step_cell<P>(L, C, o, diff, store_u, x, y, (int64_t)rec.site, df, rec.omega, true, rec, r_diff, r_norm);
+    step_cell<P>(L, C, o, diff, store_u, x, y, site_of(L, x, y), df, rec.omega, true, rec, r_diff, r_norm);
 }
 
 // ---- phase kernels.  A coarse time step is a sequence of phases; a phase
@@ -267,7 +267,7 @@ __device__ __forceinline__ int owner(const int *start, int n, int b)
 }
 
 // plain cells: blocks of a descriptor walk its active tiles
-__global__ void __launch_bounds__(256, 6) k_phase_plain(const __grid_constant__ PhaseLaunch P)
+__global__ void __launch_bounds__(256, 5) k_phase_plain(const __grid_constant__ PhaseLaunch P)
 {
     const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
     const StepDesc &d = P.d[j];
@@ -492,11 +492,34 @@ __global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int3
     }
 }
 
+// Writes populations df of cell (x, y) into the slots its next step reads at
+// parity P: its own slots (even) or the neighbours' opposite slots (odd).
+// These slots belong to the cell (AA ownership), so nothing else touches them
+// before that step.
+__device__ __forceinline__ void store_for_load(const LevelView &L, int x, int y, const float df[9], int parity)
+{
+    if (parity == 0)
+    {
+        const int64_t s = site_of(L, x, y);
+#pragma unroll
+        for (int q = 0; q < 9; q++) L.f[q * L.plane + s] = df[q];
+    }
+    else
+    {
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+        {
+            const int xs = wrapx(x - d2q9::cx(q), L.W), ys = wrapx(y - d2q9::cy(q), L.H);
+            L.f[d2q9::opp(q) * L.plane + site_of(L, xs, ys)] = df[q];
+        }
+    }
+}
+
 // Coarse buffer cells <- rescaled mean of their 4 children
 // (include/coreLB.hpp:1104-1135): f_c = f_eq,c + 2 tau_c / mean(tau_f) (mean(f_f) - f_eq,c).
 template <int PF>
 __device__ __forceinline__ void coarse_row(const LevelView &Lf, const LevelView &Lc, const Common &C,
-                                           const CoarseRowDev &row)
+                                           const CoarseRowDev &row, int pc)
 {
     float mean[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 4; k++)
@@ -520,48 +543,58 @@ __device__ __forceinline__ void coarse_row(const LevelView &Lf, const LevelView 
     const float drho = Lc.snap[row.site], ux = Lc.snap[Lc.plane + row.site], uy = Lc.snap[2 * Lc.plane + row.site];
     float feq[9];
     equilibrium(drho, C.rho0 + drho, ux, uy, feq);
+    float v[9];
 #pragma unroll
     for (int q = 0; q < 9; q++)
-        C.ibuf[(size_t)q * C.n_buf + row.buf] = feq[q] + row.ratio * (mean[q] * row.inv_nchild - feq[q]);
+    {
+        v[q] = feq[q] + row.ratio * (mean[q] * row.inv_nchild - feq[q]);
+        C.ibuf[(size_t)q * C.n_buf + row.buf] = v[q];
+    }
+    if (row.plain_target) store_for_load(Lc, row.site % Lc.pitch, row.site / Lc.pitch, v, pc);
 }
 
 // Fine buffer cells <- bicubic spline of the parent neighbourhood
 // (include/coreLB.hpp:1137-1230); the spline is linear in the node values, so
 // each child holds 6 precomputed weights.  f = f_eq + tau_f / (2 tau_c) (f_spline - f_eq).
 template <int PC>
-__device__ __forceinline__ void fine_row(const LevelView &Lf, const LevelView &Lc, const Common &C, const FineRowDev &row)
+__device__ __forceinline__ void fine_child(const LevelView &Lf, const LevelView &Lc, const Common &C,
+                                           const FineRowDev &row, int c, int pf)
 {
-    float z[6][9];
+    float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll 1
     for (int k = 0; k < 6; k++)
     {
-        if (row.node_buf[k] >= 0)
+        float z[9];
+        const int nb = row.node_buf[k];
+        if (nb >= 0)
         {
 #pragma unroll
-            for (int q = 0; q < 9; q++) z[k][q] = C.ibuf[(size_t)q * C.n_buf + row.node_buf[k]];
+            for (int q = 0; q < 9; q++) z[q] = C.ibuf[(size_t)q * C.n_buf + nb];
         }
         else
         {
             bool special;
             SpecialRec rec;
-            load_cell<PC>(Lc, C, row.node_site[k] % Lc.pitch, row.node_site[k] / Lc.pitch, 0, 0, z[k], special, rec);
+            const int ns = row.node_site[k];
+            load_cell<PC>(Lc, C, ns % Lc.pitch, ns / Lc.pitch, 0, 0, z, special, rec);
         }
+        const float w = row.weight[c][k];
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q] += w * z[q];
     }
-    for (int c = 0; c < 4; c++)
+    const int s = row.child_site[c];
+    const float drho = Lf.snap[s], ux = Lf.snap[Lf.plane + s], uy = Lf.snap[2 * Lf.plane + s];
+    float feq[9];
+    equilibrium(drho, C.rho0 + drho, ux, uy, feq);
+    const float rat = row.ratio[c];
+    const int cb = row.child_buf[c];
+#pragma unroll
+    for (int q = 0; q < 9; q++)
     {
-        const int s = row.child_site[c];
-        const float drho = Lf.snap[s], ux = Lf.snap[Lf.plane + s], uy = Lf.snap[2 * Lf.plane + s];
-        float feq[9];
-        equilibrium(drho, C.rho0 + drho, ux, uy, feq);
-        const float rat = row.ratio[c];
-#pragma unroll
-        for (int q = 0; q < 9; q++)
-        {
-            float v = 0.f;
-#pragma unroll
-            for (int k = 0; k < 6; k++) v += row.weight[c][k] * z[k][q];
-            C.ibuf[(size_t)q * C.n_buf + row.child_buf[c]] = feq[q] + rat * (v - feq[q]);
-        }
+        acc[q] = feq[q] + rat * (acc[q] - feq[q]);
+        C.ibuf[(size_t)q * C.n_buf + cb] = acc[q];
     }
+    if ((row.plain_mask >> c) & 1) store_for_load(Lf, s % Lf.pitch, s / Lf.pitch, acc, pf);
 }
 
 // One level pair of one image in the interface exchange: the two levels'
@@ -587,24 +620,28 @@ struct WaveLaunch
 };
 
 // Interface exchange wave: coarse rows of some pairs and fine rows of others
-// (independent within a wave), 128 rows per block.
+// (independent within a wave), 128 coarse rows or 32 fine rows (128 children) per block.
 __global__ void __launch_bounds__(128) k_wave(const __grid_constant__ WaveLaunch W)
 {
     const int j = owner(W.start, W.ndesc, (int)blockIdx.x);
     const PairDesc &d = W.d[j];
-    const int r = ((int)blockIdx.x - W.start[j]) * 128 + (int)threadIdx.x;
-    if (r >= d.nrows) return;
+    const int u = ((int)blockIdx.x - W.start[j]) * 128 + (int)threadIdx.x;
     if (d.kind == 0)
     {
-        const CoarseRowDev row = d.coarse[r];
-        if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row);
-        else coarse_row<0>(d.Lf, d.Lc, d.C, row);
+        // one thread per coarse row
+        if (u >= d.nrows) return;
+        const CoarseRowDev row = d.coarse[u];
+        if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row, d.pc);
+        else coarse_row<0>(d.Lf, d.Lc, d.C, row, d.pc);
     }
     else
     {
+        // one thread per fine child (4 per row)
+        const int r = u >> 2, c = u & 3;
+        if (r >= d.nrows) return;
         const FineRowDev &row = d.fine[r];
-        if (d.pc) fine_row<1>(d.Lf, d.Lc, d.C, row);
-        else fine_row<0>(d.Lf, d.Lc, d.C, row);
+        if (d.pc) fine_child<1>(d.Lf, d.Lc, d.C, row, c, d.pf);
+        else fine_child<0>(d.Lf, d.Lc, d.C, row, c, d.pf);
     }
 }
 

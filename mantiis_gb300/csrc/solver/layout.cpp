@@ -172,6 +172,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
 
     const uint32_t ALL = 0x1FFu;
     std::vector<int> spec_level;
+    std::vector<char> plain_buffer(N, 0);
     for (int64_t c = 0; c < N; c++)
     {
         int l = g.level[c];
@@ -181,10 +182,16 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         if (!(g.tau[c] > 0.0)) throw std::runtime_error("layout: non-positive relaxation time");
         const float omega = (float)(1.0 / g.tau[c]);
         uint32_t flags = 0;
-        if (buf_of[c] >= 0) flags |= SF_BUFFER;
         if (p.adsorption && c == g.inlet && g.outlet >= 0) flags |= SF_INLET;
         if (p.adsorption && c == g.outlet && g.inlet >= 0) flags |= SF_OUTLET;
         bool special = arrive[c] != ALL || wall[c] != 0 || flags != 0 || (p.adsorption && out[c] != ALL);
+        // an interpolation target that streams like a plain cell stays plain:
+        // the interface exchange writes its values into the slots it reads next
+        if (buf_of[c] >= 0)
+        {
+            if (special) flags |= SF_BUFFER;
+            else plain_buffer[c] = 1;
+        }
         if (p.adsorption)
         {
             // include/coreLB.hpp:710 (tau_d of the plain MRT from the cell's Kn)
@@ -249,7 +256,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             for (int q = 0; q < 9; q++) L.ktab.push_back((float)(p.rho0 * K[q]));
             rec.m1 |= (uint32_t)SF_HAS_K << 17;
         }
-        rec.site = s;
+        rec.xy = (int32_t)((s % lv.pitch) | ((s / lv.pitch) << 16));
         rec.omega = omega;
         lv.omega[(size_t)s] = -omega;
         L.specials.push_back(rec);
@@ -262,7 +269,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
         std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
             if (spec_level[a] != spec_level[b]) return spec_level[a] < spec_level[b];
-            return L.specials[a].site < L.specials[b].site;
+            return L.specials[a].xy < L.specials[b].xy; // row-major order
         });
         std::vector<SpecialRec> sorted(order.size());
         for (size_t i = 0; i < order.size(); i++) sorted[i] = L.specials[order[i]];
@@ -274,7 +281,8 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             LevelLayout &lv = L.levels[l - 1];
             if (lv.spec_count == 0) lv.spec_begin = (int64_t)i;
             lv.spec_count++;
-            lv.spec[(size_t)L.specials[i].site] = (uint32_t)i;
+            const int32_t xy = L.specials[i].xy;
+            lv.spec[(size_t)(xy >> 16) * lv.pitch + (xy & 0xFFFF)] = (uint32_t)i;
         }
     }
 
@@ -322,6 +330,14 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             if (g.coarse_key[r] != ckey) continue;
             const auto &row = g.coarse_rows[r];
             if (row[0] < 0 || buf_of[row[0]] < 0) continue;
+            // with three levels the reference also files some rows of the pair
+            // (l2, l2 + 1) under this key (target one level up); the same target
+            // has its row under the right key, which is processed later and sets
+            // the final value, so the stray copy is left out
+            bool same_levels = g.level[row[0]] == l2;
+            for (int k = 1; k < 5; k++)
+                if (row[k] >= 0 && g.level[row[k]] != l1) same_levels = false;
+            if (!same_levels) continue;
             CoarseRowDev d{};
             d.site = L.cell_site[row[0]];
             d.buf = buf_of[row[0]];
@@ -341,6 +357,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             if (cnt == 0) continue;
             d.ratio = (float)(2 * g.tau[row[0]] / (tsum / cnt));
             d.inv_nchild = 1.0f / cnt;
+            d.plain_target = plain_buffer[row[0]];
             itf.coarse.push_back(d);
         }
         const int top_order[9] = {7, 4, 8, 3, 0, 1, 6, 2, 5};
@@ -398,6 +415,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
                 int64_t ch = row[k + 1];
                 d.child_site[k] = L.cell_site[ch];
                 d.child_buf[k] = buf_of[ch];
+                if (plain_buffer[ch]) d.plain_mask |= 1 << k;
                 double w[6];
                 spline_weights(xnode, ynode, g.x[ch] + child_shift + 1, g.y[ch] + child_shift + 1, w);
                 double sum = 0;

@@ -37,7 +37,9 @@ enum CollisionMode
 // flags of a special cell record
 enum SpecialFlags : uint32_t
 {
-    SF_BUFFER = 1u,   // multi-block buffer cell: first substep of a coarse step reads the interpolated values
+    SF_BUFFER = 1u,   // multi-block buffer cell that is special anyway: the first substep of a coarse step
+                      // reads the interpolated values from the interpolation buffer (a buffer cell
+                      // that is otherwise plain gets them written into the slots it reads)
     SF_INLET = 2u,    // adsorption inlet (include/coreLB.hpp:980-1009)
     SF_OUTLET = 4u,
     SF_HAS_K = 8u,    // has a constant term row in the K table
@@ -57,7 +59,7 @@ struct alignas(16) SpecialRec
     int32_t quirk_base;// side-buffer slot of this cell's first quirk link
     int32_t k_row;     // row of the constant-term table (SF_HAS_K)
     int32_t buf;       // interpolation buffer index (SF_BUFFER), else -1
-    int32_t site;      // site of the cell on its level
+    int32_t xy;        // position of the cell on its level: x | y << 16
     float omega;       // 1/tau_s of the cell
 };
 
@@ -88,6 +90,8 @@ struct CoarseRowDev
     int32_t child_buf[4];// >= 0: read that child from the interpolation buffer (it was refreshed earlier in this phase)
     float ratio;         // 2 tau_c / mean(tau_children)
     float inv_nchild;    // 1 / number of children present
+    int32_t plain_target;// the coarse cell steps as a plain cell: its values also go to the slots it reads next
+    int32_t pad_;
 };
 
 // Fine-buffer row: 4 fine buffer cells <- spline of the parent neighbourhood
@@ -99,6 +103,8 @@ struct FineRowDev
     int32_t child_buf[4];
     float weight[4][6];  // interpolation weights per child
     float ratio[4];      // tau_child / (2 tau_parent)
+    int32_t plain_mask;  // bit c: child c steps as a plain cell (values also go to the slots it reads next)
+    int32_t pad_[3];
 };
 
 struct InterfaceLayout

@@ -618,7 +618,7 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
         {
             d.kind = 1;
             d.nrows = it.nfine;
-            wv[it.l1].push_back({d, (it.nfine + 127) / 128});
+            wv[it.l1].push_back({d, (4 * it.nfine + 127) / 128});
         }
     }
     V.waves.resize(P.nwave);

@@ -168,5 +168,6 @@ def test_batch_matches_single_contexts(fixture64):
         assert np.array_equal(s.cells(with_f=True)["f"], g.cells(with_f=True)["f"])
     obs = b.observables()
     for s, o in zip(solo, obs):
-        assert o["mean_ux"] == s.observables()["mean_ux"]
+        # same state; the FP64 block sums are added atomically (order varies)
+        assert abs(o["mean_ux"] - s.observables()["mean_ux"]) <= 1e-12 * abs(o["mean_ux"])
     assert b.launches > 0
