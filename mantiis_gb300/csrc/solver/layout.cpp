@@ -97,7 +97,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         lv.pitch = ((lv.W + 31) / 32) * 32;
         lv.plane = (int64_t)lv.pitch * lv.H;
         lv.omega.assign((size_t)lv.plane, 0.0f);
-        if (p.adsorption) lv.tau_d.assign((size_t)lv.plane, 0.0f);
+        if (p.adsorption || p.collision == COLL_MRT) lv.tau_d.assign((size_t)lv.plane, 0.0f);
         lv.spec.assign((size_t)lv.plane, 0u);
         lv.substeps = 1 << (ML - l);
         lv.snapshot_all = g.multiblock;
@@ -192,7 +192,7 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
             if (special) flags |= SF_BUFFER;
             else plain_buffer[c] = 1;
         }
-        if (p.adsorption)
+        if (p.adsorption || p.collision == COLL_MRT)
         {
             // include/coreLB.hpp:710 (tau_d of the plain MRT from the cell's Kn)
             double a = p.mfp_over_cl * 1.0 / (1.0 + 2.0 * g.kn[c]);

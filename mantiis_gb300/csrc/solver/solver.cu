@@ -796,9 +796,9 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
             d.snap.alloc((size_t)ll.plane * 3, acct);
             d.snap.zero(s);
         }
+        if (!ll.tau_d.empty()) d.tau2.upload(ll.tau_d, acct, s); // plain MRT: tau_d from Kn
         if (ctx->adsorption)
         {
-            d.tau2.upload(ll.tau_d, acct, s);
             d.psi.alloc((size_t)ll.plane, acct);
             d.psi.zero(s);
             d.rho_prev.alloc((size_t)ll.plane, acct);

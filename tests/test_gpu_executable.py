@@ -1,0 +1,61 @@
+"""The drop-in executable (mantiis_gb300/bin/mantiis) with the reference's
+argument interface and file layout (include/mantiisApp.hpp:131-142, 398-428):
+inputs pore.dat / Kn.dat / localporesize.dat (column-major), outputs
+ux.txt uy.txt rho.txt f.txt convergence.txt SimulationDetails.txt in the input
+folder and reconstructed.dat in the working directory, compared with the
+reference's gold files (test/run_tests.sh cases, 64x64, 100 steps)."""
+import subprocess
+
+import numpy as np
+import pytest
+from conftest import ROOT
+
+BIN = ROOT / "mantiis_gb300" / "bin" / "mantiis"
+
+
+def write_inputs(folder, fx):
+    # the reference reads N*N numbers per file, x-major (column-major of [y, x])
+    np.savetxt(folder / "pore.dat", np.asarray(fx["pore"]).T.reshape(-1), fmt="%d")
+    np.savetxt(folder / "Kn.dat", np.asarray(fx["kn"]).T.reshape(-1), fmt="%.17g")
+    np.savetxt(folder / "localporesize.dat", np.asarray(fx["locpore"]).T.reshape(-1), fmt="%.17g")
+
+
+def test_usage_and_exit_code():
+    # fewer than 6 arguments: usage on stderr, exit code 1 (include/mantiisApp.hpp:131-135)
+    r = subprocess.run([str(BIN), "1", "False"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "Usage:" in r.stderr and "<input_folder/>" in r.stderr
+
+
+def test_missing_input_folder(tmp_path):
+    r = subprocess.run([str(BIN), "1", "False", "64", str(tmp_path / "absent") + "/", "10"], capture_output=True,
+                       text=True, timeout=120, cwd=tmp_path)
+    assert r.returncode != 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,preset", [("transport", "transport_test"), ("adsorption", "adsorption_test")])
+def test_executable_matches_gold(tmp_path, fixture64, case, preset):
+    folder = tmp_path / "io"
+    folder.mkdir()
+    write_inputs(folder, fixture64)
+    r = subprocess.run([str(BIN), "1", "False", "64", str(folder) + "/", "100", "--preset", preset],
+                       capture_output=True, text=True, timeout=600, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    ux = np.loadtxt(folder / "ux.txt").reshape(64, 64)
+    uy = np.loadtxt(folder / "uy.txt").reshape(64, 64)
+    rho = np.loadtxt(folder / "rho.txt").reshape(64, 64)
+    umax = np.abs(fixture64[f"{case}_ux"]).max()
+    e_ux = np.abs(ux - fixture64[f"{case}_ux"]).max() / umax
+    e_uy = np.abs(uy - fixture64[f"{case}_uy"]).max() / umax
+    e_rho = np.abs(rho - fixture64[f"{case}_rho"]).max() / np.abs(fixture64[f"{case}_rho"]).max()
+    # the same bounds as the library-level gold tests
+    if case == "transport":
+        assert e_ux < 1e-4 and e_uy < 1e-4 and e_rho < 1e-6
+    else:
+        assert e_ux < 1e-3 and e_uy < 1e-3 and e_rho < 1e-4
+    assert len(np.loadtxt(folder / "convergence.txt")) == 100
+    assert np.loadtxt(folder / "f.txt").size == 64 * 64 * 9
+    assert (folder / "SimulationDetails.txt").read_text().count("\n") >= 4
+    assert (tmp_path / "reconstructed.dat").exists()
+    assert "Timestep:" in r.stdout

@@ -171,3 +171,22 @@ def test_batch_matches_single_contexts(fixture64):
         # same state; the FP64 block sums are added atomically (order varies)
         assert abs(o["mean_ux"] - s.observables()["mean_ux"]) <= 1e-12 * abs(o["mean_ux"])
     assert b.launches > 0
+
+
+# collision 0 BGK, 1 MRT, 2 regularized MRT; wall 0 BB, 1 MDBB, 2 SRBB
+# (include/coreLB.hpp:678-792, 859-967): the variants the reference selects with
+# Settings::collision_method / wall_boundary, checked against the FP64 oracle
+@pytest.mark.parametrize("collision,wall,multiblock", [(2, 1, 0), (1, 2, 0), (0, 0, 0), (1, 1, 0), (2, 1, 1), (0, 2, 1)])
+def test_collision_and_wall_variants_vs_oracle(fixture64, collision, wall, multiblock):
+    p = default_params(dx=1e-9, collision=collision, wall=wall, multiblock=multiblock)
+    g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    o = for_grid(g, sim="transport", dx=1e-9, collision=collision, wall=wall)
+    o.run(60)
+    ref = o.fields()
+    s = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    s.advance(60)
+    got = s.cells(with_f=True)
+    e = rel_err(got["ux"], ref["ux"])
+    e_f = np.abs(got["f"] - ref["f"]).max() / 0.2355
+    record(f"variant_c{collision}_w{wall}_mb{multiblock}", ux=e, f=e_f)
+    assert e < 1e-4 and e_f < 1e-6
