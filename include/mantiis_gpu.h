@@ -237,6 +237,15 @@ int mgpu_pore_properties(const int32_t *pore, int n, double dx, double mfp, doub
 /* Seeded disk packing (synthetic pore images): disks of radius U[rmin, rmax]
  * at uniform centres until the porosity is <= porosity; rows 0 and n-1 solid. */
 int mgpu_generate_disks(int n, double rmin, double rmax, double porosity, uint64_t seed, int32_t *pore_out);
+/* Same with flags: MGPU_DISKS_PERIODIC_X makes the disks wrap across the
+ * x-periodic edge, so the image is itself x-periodic; MGPU_DISKS_OPEN_X_EDGES
+ * keeps the two columns at either x edge void (solid pixels on the x-periodic
+ * seam make the reference's wall-then-periodic order lose mass there, so such
+ * images have no steady state). */
+#define MGPU_DISKS_PERIODIC_X 1
+#define MGPU_DISKS_OPEN_X_EDGES 2
+int mgpu_generate_disks_ex(int n, double rmin, double rmax, double porosity, uint64_t seed, int flags,
+                           int32_t *pore_out);
 
 #ifdef __cplusplus
 }

@@ -236,9 +236,17 @@ int mgpu_pore_properties(const int32_t *pore, int n, double dx, double mfp, doub
 
 int mgpu_generate_disks(int n, double rmin, double rmax, double porosity, uint64_t seed, int32_t *pore_out)
 {
+    return mgpu_generate_disks_ex(n, rmin, rmax, porosity, seed, 0, pore_out);
+}
+
+int mgpu_generate_disks_ex(int n, double rmin, double rmax, double porosity, uint64_t seed, int flags,
+                           int32_t *pore_out)
+{
     return host_guard([&]() {
         if (!pore_out || n <= 0 || rmin <= 0 || rmax < rmin) throw std::invalid_argument("bad argument");
-        std::vector<int> img = generate_disk_image(n, rmin, rmax, porosity, seed);
+        std::vector<int> img =
+            generate_disk_image(n, rmin, rmax, porosity, seed, (flags & MGPU_DISKS_PERIODIC_X) != 0,
+                                (flags & MGPU_DISKS_OPEN_X_EDGES) != 0);
         std::copy(img.begin(), img.end(), pore_out);
         return MGPU_OK;
     });

@@ -322,7 +322,8 @@ int64_t fill_untabulated_pixels(std::vector<int> &img, int n)
     return filled;
 }
 
-std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed)
+std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed, bool periodic_x,
+                                     bool open_x_edges)
 {
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<double> ur(rmin, rmax), uc(0.0, (double)n);
@@ -340,11 +341,25 @@ std::vector<int> generate_disk_image(int n, double rmin, double rmax, double por
     {
         double r = ur(rng), cx = uc(rng), cy = uc(rng);
         int r0 = std::max(0, (int)std::floor(cy - r)), r1 = std::min(n - 1, (int)std::ceil(cy + r));
-        int c0 = std::max(0, (int)std::floor(cx - r)), c1 = std::min(n - 1, (int)std::ceil(cx + r));
+        int c0 = (int)std::floor(cx - r), c1 = (int)std::ceil(cx + r);
+        if (!periodic_x)
+        {
+            c0 = std::max(0, c0);
+            c1 = std::min(n - 1, c1);
+        }
+        else if (c1 - c0 >= n)
+        {
+            c0 = 0;
+            c1 = n - 1;
+        }
         for (int i = r0; i <= r1; i++)
-            for (int j = c0; j <= c1; j++)
+            for (int jj = c0; jj <= c1; jj++)
             {
-                double dy = i - cy, dxv = j - cx;
+                // x-periodic disks also cover the columns they reach across the edge
+                const int j = ((jj % n) + n) % n;
+                if (open_x_edges && (j < 2 || j >= n - 2)) continue;
+                double dy = i - cy, dxv = std::fabs(j - cx);
+                if (periodic_x) dxv = std::min(dxv, (double)n - dxv);
                 if (dy * dy + dxv * dxv <= r * r && img[(size_t)i * n + j])
                 {
                     img[(size_t)i * n + j] = 0;

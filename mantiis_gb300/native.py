@@ -114,6 +114,7 @@ SIGNATURES = {
     "mgpu_units": (C.c_int, [C.c_double, C.c_double, C.c_double, F64P]),
     "mgpu_pore_properties": (C.c_int, [I32P, C.c_int, C.c_double, C.c_double, F64P, F64P]),
     "mgpu_generate_disks": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, I32P]),
+    "mgpu_generate_disks_ex": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int, I32P]),
 }
 
 
@@ -167,9 +168,12 @@ def pore_properties(pore, dx, mfp):
     return lp, kn
 
 
-def generate_disks(n, rmin, rmax, porosity, seed):
+def generate_disks(n, rmin, rmax, porosity, seed, periodic_x=False, open_x_edges=False):
+    """Seeded disk packing; periodic_x wraps the disks across the x-periodic
+    edge, open_x_edges keeps the two columns at either x edge void."""
     out = np.zeros(n * n, dtype=np.int32)
-    _host_check(lib().mgpu_generate_disks(n, rmin, rmax, porosity, seed, out))
+    flags = (1 if periodic_x else 0) | (2 if open_x_edges else 0)
+    _host_check(lib().mgpu_generate_disks_ex(n, rmin, rmax, porosity, seed, flags, out))
     return out.reshape(n, n)
 
 
