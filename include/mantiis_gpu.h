@@ -56,6 +56,9 @@ typedef struct mgpu_params
     int edge_fine;         /* 1: keep the quadtree at the finest level on the x-periodic edges (the
                               reference's grid, 0, leaves coarse/fine interfaces across that boundary
                               without buffer cells, which makes the multi-block solution diverge) */
+    int plain_path;        /* plain cells of x-interior tiles: 1 = TMA pipeline through shared memory
+                              (default), 0 = direct loads; -1 = pick the faster per image by timing
+                              both at creation (autotune) */
 } mgpu_params;
 
 /* Static description of a built context. */

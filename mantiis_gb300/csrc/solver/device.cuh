@@ -339,13 +339,13 @@ template <int P> __device__ __forceinline__ float wall_slot(const LevelView &L, 
 
 // Populations of a special cell after streaming and the wall rules:
 //   stream (=) -> wall (SRBB +=, BB/MDBB =) -> x-periodic (=) -> inlet/outlet (=)
-// (include/mantiisApp.hpp:239-265, include/coreLB.hpp:834-1009).
-template <int P>
-__device__ __forceinline__ void load_special(const LevelView &L, const Common &C, const SpecialRec &rec, int x, int y,
-                                             float df[9])
+// (include/mantiisApp.hpp:239-265, include/coreLB.hpp:834-1009).  `raw` holds
+// the slots the cell reads at parity P; `wall(q)` gives the value its wall
+// link q left in the previous step.
+template <int P, typename WallSlot>
+__device__ __forceinline__ void special_rules(const Common &C, const SpecialRec &rec, const float raw[9], WallSlot wall_of,
+                                              float df[9])
 {
-    float raw[9];
-    load_raw<P>(L, x, y, raw);
     const uint32_t arrive = rec.m0 & 0x1FFu, over = (rec.m0 >> 9) & 0x1FFu, wall = (rec.m0 >> 18) & 0x1FFu;
     const uint32_t quirk = rec.m1 & 0x1FFu, bnd = (rec.m1 >> 9) & 0xFFu, flags = (rec.m1 >> 17) & 0xFu;
 #pragma unroll
@@ -355,18 +355,24 @@ __device__ __forceinline__ void load_special(const LevelView &L, const Common &C
         const float r = rec.r;
         int qi = 0;
         const float *side_prev = C.side + (size_t)(P ^ 1) * C.n_quirk;
+        // unrolled with fixed indices (the specular target is matched against
+        // each population), so df stays in registers
+#pragma unroll
         for (int q = 0; q < 9; q++)
         {
             if (!((wall >> q) & 1u)) continue;
             float v;
             if ((quirk >> q) & 1u) v = side_prev[rec.quirk_base + qi++];
-            else v = wall_slot<P>(L, x, y, q);
+            else v = wall_of(q);
             const int p1 = d2q9::opp(q);
             if (C.wall == WALL_SRBB)
             {
                 const int p2 = (bnd == 0xFFu) ? p1 : (int)c_icsr[bnd * 9 + q];
                 if (!((over >> p1) & 1u)) df[p1] += r * v;
-                if (!((over >> p2) & 1u)) df[p2] += (1.0f - r) * v;
+                const float rv = (((over >> p2) & 1u) ? 0.0f : (1.0f - r) * v);
+#pragma unroll
+                for (int p = 0; p < 9; p++)
+                    if (p == p2) df[p] += rv;
             }
             else if (!((over >> p1) & 1u))
                 df[p1] = v;
@@ -388,6 +394,15 @@ __device__ __forceinline__ void load_special(const LevelView &L, const Common &C
         df[3] = C.inlet_axis;
         df[6] = df[7] = C.inlet_diag;
     }
+}
+
+template <int P>
+__device__ __forceinline__ void load_special(const LevelView &L, const Common &C, const SpecialRec &rec, int x, int y,
+                                             float df[9])
+{
+    float raw[9];
+    load_raw<P>(L, x, y, raw);
+    special_rules<P>(C, rec, raw, [&](int q) { return wall_slot<P>(L, x, y, q); }, df);
 }
 } // namespace dev
 } // namespace mantiis

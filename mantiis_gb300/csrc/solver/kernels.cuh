@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "device.cuh"
+#include "tma.cuh"
 
 namespace mantiis
 {
@@ -175,7 +176,9 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
 // link): one thread per site of a 32x8 tile, the row masks of plain cells let
 // the relaxation rate and the nine populations load together.  Each slot a
 // thread reads is written by that thread alone in this launch (AA ownership),
-// so the loads take the read-only path.
+// so the loads take the read-only path.  Special cells (walls, missing
+// arrivals, buffers) go to their own kernel: in the same warps their longer
+// path would hold the plain lanes.
 template <int P>
 __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, const StepOpt &o, int t, int diff,
                                            int store_u, double &r_diff, double &r_norm)
@@ -237,7 +240,7 @@ struct StepDesc
     StepOpt o;
     int64_t spec_begin; // the level's special records
     int spec_count;
-    int pad_;
+    int tile_base;      // first tile of the level's list this descriptor covers
 };
 
 // Per-launch residual switches: the residual terms (and the |u| store) apply
@@ -266,12 +269,12 @@ __device__ __forceinline__ int owner(const int *start, int n, int b)
     return j;
 }
 
-// plain cells: blocks of a descriptor walk its active tiles
+// plain cells with direct loads: blocks of a descriptor walk its tiles
 __global__ void __launch_bounds__(256, 5) k_phase_plain(const __grid_constant__ PhaseLaunch P)
 {
     const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
     const StepDesc &d = P.d[j];
-    const int t = (int)blockIdx.x - P.start[j];
+    const int t = d.tile_base + (int)blockIdx.x - P.start[j];
     const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
     double r_diff = 0.0, r_norm = 0.0;
     if (d.o.parity) plain_tile<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
@@ -293,6 +296,134 @@ __global__ void __launch_bounds__(128) k_phase_special(const __grid_constant__ P
         else special_cell<0>(d.L, d.C, d.o, d.spec_begin + i, diff, store_u, r_diff, r_norm);
     }
     if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
+}
+
+// ---- plain cells through a TMA pipeline.  A persistent block walks the
+// x-interior tiles of its descriptors; for each tile one bulk tensor copy
+// brings the 9 planes with a halo of 4 columns and 1 row (a 40 x 10 x 9 box,
+// x start 16-byte aligned), a second the tile's 32 x 8 relaxation rates and a
+// bulk copy its 8 row masks into shared memory, two tiles ahead of the one
+// being stepped.  Cells read their slots from shared memory (odd steps index
+// the shifted neighbours there) and store as in plain_tile.
+constexpr int kTmaW = 40, kTmaH = 10, kTmaStages = 2;
+constexpr uint32_t kTmaFBytes = kTmaW * kTmaH * 9 * 4;
+constexpr uint32_t kTmaOmOff = (kTmaFBytes + 127) / 128 * 128; // 128-byte aligned
+constexpr uint32_t kTmaMaskOff = kTmaOmOff + 32 * 8 * 4;
+constexpr uint32_t kTmaTxBytes = kTmaFBytes + 32 * 8 * 4 + 32;         // bytes the copies of one tile deliver
+constexpr uint32_t kTmaStageBytes = (kTmaMaskOff + 32 + 127) / 128 * 128; // stage stride
+constexpr int kMaxTmaDescs = 8;
+constexpr uint32_t kWaitPolls = 1u << 26;
+
+struct TmaLaunch
+{
+    CUtensorMap map[kMaxTmaDescs];    // per descriptor: its level's 9 planes as (x, y, q)
+    CUtensorMap om_map[kMaxTmaDescs]; // per descriptor: its level's relaxation rates as (x, y)
+    int grid;                         // persistent blocks of the launch (host side)
+    int ndesc;
+    int start[kMaxTmaDescs + 1];      // first tile (in launch order) of each descriptor
+    PhaseArgs a;
+    StepDesc d[kMaxTmaDescs];
+};
+
+template <int P>
+__device__ __forceinline__ void plain_tile_smem(const LevelView &L, const Common &C, const StepOpt &o, int tile,
+                                                const unsigned char *stage, int diff, int store_u, double &r_diff,
+                                                double &r_norm)
+{
+    const float *sb = reinterpret_cast<const float *>(stage);
+    const float *som = reinterpret_cast<const float *>(stage + kTmaOmOff);
+    const uint32_t *smask = reinterpret_cast<const uint32_t *>(stage + kTmaMaskOff);
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    if (!((smask[ly] >> lx) & 1u)) return;
+    const int x = (tile & 0xFFFF) * 32 + lx, y = (tile >> 16) * 8 + ly;
+    const int64_t s = site_of(L, x, y);
+    const float om = som[ly * 32 + lx];
+    float df[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+    {
+        // even: own slot (x, q); odd: slot (x - c_q, opp q)
+        const int pq = P == 0 ? q : d2q9::opp(q);
+        const int sy = ly + 1 - (P == 0 ? 0 : d2q9::cy(q)), sx = lx + 4 - (P == 0 ? 0 : d2q9::cx(q));
+        df[q] = sb[(pq * kTmaH + sy) * kTmaW + sx];
+    }
+    SpecialRec none;
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, true);
+}
+
+__global__ void __launch_bounds__(256, 4) k_phase_plain_tma(const __grid_constant__ TmaLaunch P)
+{
+    __shared__ __align__(128) unsigned char sbuf[kTmaStages][kTmaStageBytes];
+    __shared__ __align__(8) uint64_t full[kTmaStages];
+    __shared__ int s_tile[kTmaStages];
+    __shared__ int s_fail;
+    static_assert(kTmaStageBytes % 128 == 0 && kTmaOmOff % 128 == 0 && kTmaMaskOff % 16 == 0, "stage layout");
+    const int total = P.start[P.ndesc];
+    if (threadIdx.x == 0)
+    {
+        for (int st = 0; st < kTmaStages; st++) mbar_init(&full[st], 1);
+        s_fail = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](int g, int st) {
+        const int j = owner(P.start, P.ndesc, g);
+        const int t = P.d[j].tile_base + g - P.start[j];
+        const int tile = P.d[j].L.tiles[t];
+        const int x0 = (tile & 0xFFFF) * 32, y0 = (tile >> 16) * 8;
+        s_tile[st] = tile;
+        mbar_arrive_expect_tx(&full[st], kTmaTxBytes);
+        tma_load_3d(sbuf[st], &P.map[j], x0 - 4, y0 - 1, 0, &full[st]);
+        tma_load_2d(sbuf[st] + kTmaOmOff, &P.om_map[j], x0, y0, &full[st]);
+        bulk_load(sbuf[st] + kTmaMaskOff, P.d[j].L.tile_mask + (size_t)t * 8, 32, &full[st]);
+    };
+    if (threadIdx.x == 0)
+        for (int st = 0; st < kTmaStages; st++)
+        {
+            const int g = (int)blockIdx.x + st * (int)gridDim.x;
+            if (g < total) issue(g, st);
+        }
+    double r_diff = 0.0, r_norm = 0.0;
+    int red_desc = -1;
+    int it = 0;
+    for (int g = (int)blockIdx.x; g < total; g += (int)gridDim.x, it++)
+    {
+        const int st = it % kTmaStages;
+        const uint32_t parity = (uint32_t)(it / kTmaStages) & 1u;
+        if (!mbar_wait_bounded(&full[st], parity, kWaitPolls)) atomicOr(&s_fail, 1);
+        __syncthreads();
+        if (s_fail) break;
+        const int j = owner(P.start, P.ndesc, g);
+        const StepDesc &d = P.d[j];
+        const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
+        if (diff) red_desc = j;
+        const int tile = s_tile[st];
+        if (d.o.parity) plain_tile_smem<1>(d.L, d.C, d.o, tile, sbuf[st], diff, store_u, r_diff, r_norm);
+        else plain_tile_smem<0>(d.L, d.C, d.o, tile, sbuf[st], diff, store_u, r_diff, r_norm);
+        // every thread is done with this stage before it is refilled
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            const int gn = g + kTmaStages * (int)gridDim.x;
+            if (gn < total) issue(gn, st);
+        }
+    }
+    if (s_fail)
+    {
+        if (threadIdx.x == 0)
+        {
+            atomicOr(P.d[0].C.err, kErrTmaTimeout);
+            // let copies still in flight land before the block's shared memory goes
+            for (int st = 0; st < kTmaStages; st++) mbar_wait_bounded(&full[st], 0u, 1024u);
+        }
+        return;
+    }
+    // residual terms: only single-image launches ask for them (one accumulator)
+    if (P.a.diff)
+    {
+        const int rd = __syncthreads_or(red_desc >= 0) ? 0 : -1;
+        if (rd == 0) block_add2(r_diff, r_norm, P.d[0].C.red + P.a.red_slot);
+    }
 }
 
 // Maximum of a non-negative double over the block, then one atomic per block

@@ -286,34 +286,44 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         }
     }
 
-    // active tiles (32 x 8 sites)
+    // active tiles (32 x 8 sites): the x-interior ones first, then the two
+    // border columns
     for (auto &lv : L.levels)
     {
-        for (int ty = 0; ty < lv.tiles_y; ty++)
-            for (int tx = 0; tx < lv.tiles_x; tx++)
-            {
-                bool any = false;
-                for (int yy = ty * 8; yy < std::min(lv.H, ty * 8 + 8) && !any; yy++)
-                    for (int xx = tx * 32; xx < std::min(lv.W, tx * 32 + 32); xx++)
-                        if (lv.omega[(size_t)yy * lv.pitch + xx] != 0.0f)
-                        {
-                            any = true;
-                            break;
-                        }
-                if (!any) continue;
-                lv.tile_list.push_back(tx | ty << 16);
-                for (int r = 0; r < 8; r++)
+        std::vector<std::pair<int, int>> order;
+        for (int pass = 0; pass < 2; pass++)
+            for (int ty = 0; ty < lv.tiles_y; ty++)
+                for (int tx = 0; tx < lv.tiles_x; tx++)
                 {
-                    uint32_t m = 0;
-                    int yy = ty * 8 + r;
-                    for (int k = 0; k < 32 && yy < lv.H; k++)
-                    {
-                        int xx = tx * 32 + k;
-                        if (xx < lv.W && lv.omega[(size_t)yy * lv.pitch + xx] > 0.0f) m |= 1u << k;
-                    }
-                    lv.tile_mask.push_back(m);
+                    const bool interior = tx > 0 && tx + 1 < lv.tiles_x;
+                    if (interior == (pass == 0)) order.push_back({tx, ty});
                 }
+        for (const auto &tt : order)
+        {
+            const int tx = tt.first, ty = tt.second;
+            bool any = false;
+            for (int yy = ty * 8; yy < std::min(lv.H, ty * 8 + 8) && !any; yy++)
+                for (int xx = tx * 32; xx < std::min(lv.W, tx * 32 + 32); xx++)
+                    if (lv.omega[(size_t)yy * lv.pitch + xx] != 0.0f)
+                    {
+                        any = true;
+                        break;
+                    }
+            if (!any) continue;
+            if (tx > 0 && tx + 1 < lv.tiles_x) lv.n_tiles_interior++;
+            lv.tile_list.push_back(tx | ty << 16);
+            for (int r = 0; r < 8; r++)
+            {
+                uint32_t m = 0;
+                int yy = ty * 8 + r;
+                for (int k = 0; k < 32 && yy < lv.H; k++)
+                {
+                    int xx = tx * 32 + k;
+                    if (xx < lv.W && lv.omega[(size_t)yy * lv.pitch + xx] > 0.0f) m |= 1u << k;
+                }
+                lv.tile_mask.push_back(m);
             }
+        }
     }
 
     // interfaces (include/coreLB.hpp:1101-1231)

@@ -72,7 +72,8 @@ struct LevelLayout
     std::vector<float> omega;        // per site 1/tau_s: 0 inactive, >0 plain, <0 special
     std::vector<float> tau_d;        // per site tau_d of the plain MRT (adsorption), else empty
     std::vector<uint32_t> spec;      // per site: special record index (valid when tau < 0)
-    std::vector<int32_t> tile_list;  // active 32x8 tiles: tx | ty << 16
+    std::vector<int32_t> tile_list;  // active 32x8 tiles: tx | ty << 16; x-interior tiles first
+    int n_tiles_interior = 0;        // tiles with tx in [1, tiles_x - 2] (no x wrap within one cell)
     std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
     int tiles_x = 0, tiles_y = 0;
     int64_t n_active = 0, n_active_real = 0;
@@ -91,8 +92,9 @@ struct CoarseRowDev
     float ratio;         // 2 tau_c / mean(tau_children)
     float inv_nchild;    // 1 / number of children present
     int32_t plain_target;// the coarse cell steps as a plain cell: its values also go to the slots it reads next
-    int32_t pad_;
+    int32_t pad_[3];     // 64 bytes: rows stay 16-byte aligned in an array
 };
+static_assert(sizeof(CoarseRowDev) % 16 == 0, "coarse row size");
 
 // Fine-buffer row: 4 fine buffer cells <- spline of the parent neighbourhood
 struct FineRowDev
@@ -106,6 +108,7 @@ struct FineRowDev
     int32_t plain_mask;  // bit c: child c steps as a plain cell (values also go to the slots it reads next)
     int32_t pad_[3];
 };
+static_assert(sizeof(FineRowDev) % 16 == 0, "fine row size");
 
 struct InterfaceLayout
 {

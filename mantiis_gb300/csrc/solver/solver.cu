@@ -1,5 +1,7 @@
 // Host context of the GB300 lattice Boltzmann solver and its C ABI
 // (include/mantiis_gpu.h).  One context = one pore image on one GPU stream.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +31,10 @@ namespace
 thread_local std::string g_error;
 
 struct CudaError : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+struct DeviceError : std::runtime_error
 {
     using std::runtime_error::runtime_error;
 };
@@ -98,6 +104,9 @@ template <typename T> struct DevBuf
 
 struct LevelDev
 {
+    CUtensorMap tmap;    // the 9 planes as a (x, y, q) tensor for the TMA tile loads
+    CUtensorMap om_map;  // the relaxation rates as a (x, y) tensor
+    bool has_tmap = false;
     DevBuf<float> f, omega, tau2, snap, unorm, psi, rho_prev;
     DevBuf<uint32_t> spec;
     DevBuf<int32_t> tiles;
@@ -120,7 +129,9 @@ constexpr int kRing = 8192; // residual accumulator slots (4 doubles each)
 // kMaxPhaseDescs level descriptors), per interface wave its launches.
 struct PhaseVariant
 {
-    std::vector<std::vector<dev::PhaseLaunch>> plain, spec; // per phase
+    std::vector<std::vector<dev::PhaseLaunch>> plain; // per phase: plain cells, tiles with direct loads
+    std::vector<std::vector<dev::TmaLaunch>> tma;     // per phase: plain cells, x-interior tiles through TMA
+    std::vector<std::vector<dev::PhaseLaunch>> spec;  // per phase: special cells
     std::vector<std::vector<dev::WaveLaunch>> waves;        // per wave
 };
 
@@ -270,6 +281,10 @@ template <typename F> int guarded(mgpu_ctx *ctx, F &&fn)
     {
         return fail(ctx, MGPU_E_CUDA, e.what());
     }
+    catch (const DeviceError &e)
+    {
+        return fail(ctx, MGPU_E_DEVICE, e.what());
+    }
     catch (const InputError &e)
     {
         return fail(ctx, MGPU_E_INPUT, e.what());
@@ -288,6 +303,49 @@ template <typename F> int guarded(mgpu_ctx *ctx, F &&fn)
     {
         return fail(ctx, MGPU_E_ARG, e.what());
     }
+}
+
+// cuTensorMapEncodeTiled from the driver, through the runtime's entry-point
+// query (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn)
+    {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p) throw std::runtime_error("cuTensorMapEncodeTiled is not available");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// the level's 9 planes as a 3-D tensor (x: pitch floats, y: H rows, q: 9
+// planes) read in boxes of 40 x 10 x 9 (a 32 x 8 tile with its halo)
+// the level's relaxation-rate plane, read in 32 x 8 boxes (one tile)
+void encode_omega_map(CUtensorMap *map, const float *om, const LevelLayout &ll)
+{
+    const cuuint64_t dims[2] = {(cuuint64_t)ll.pitch, (cuuint64_t)ll.H};
+    const cuuint64_t strides[1] = {(cuuint64_t)ll.pitch * 4};
+    const cuuint32_t box[2] = {32, 8};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(om), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+void encode_level_map(CUtensorMap *map, float *f, const LevelLayout &ll)
+{
+    const cuuint64_t dims[3] = {(cuuint64_t)ll.pitch, (cuuint64_t)ll.H, 9};
+    const cuuint64_t strides[2] = {(cuuint64_t)ll.pitch * 4, (cuuint64_t)ll.plane * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)dev::kTmaW, (cuuint32_t)dev::kTmaH, 9};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = tensor_map_encoder()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, f, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
 
 void upload_constants()
@@ -310,6 +368,20 @@ void upload_constants()
     CK(cudaMemcpyToSymbol(dev::c_nneg, nneg, sizeof(nneg)));
 }
 
+// device error word (a bounded wait that ran out, ...): raises MGPU_E_DEVICE
+void check_device_error(mgpu_ctx *ctx)
+{
+    unsigned int w = 0;
+    CK(cudaMemcpyAsync(&w, ctx->errword.p, sizeof(w), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (w)
+    {
+        CK(cudaMemsetAsync(ctx->errword.p, 0, sizeof(w), ctx->stream));
+        throw DeviceError("device error flag " + std::to_string(w) +
+                          ((w & dev::kErrTmaTimeout) ? ": a tile copy did not complete in time" : ""));
+    }
+}
+
 void launch_check(mgpu_ctx *ctx)
 {
     ctx->launches++;
@@ -322,9 +394,9 @@ void launch_check(mgpu_ctx *ctx)
 std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int only_level);
 std::string state_key(const std::vector<mgpu_ctx *> &ctxs, int ahead);
 PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, int ahead);
-void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::PhaseLaunch> &spec,
-                  const dev::PhaseArgs &a, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
-                  int64_t &launches);
+void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::TmaLaunch> &tma,
+                  const std::vector<dev::PhaseLaunch> &spec, const dev::PhaseArgs &a, cudaStream_t main,
+                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int64_t &launches);
 void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, cudaStream_t side,
                 cudaEvent_t fork, cudaEvent_t join, dev::PhaseArgs a, int64_t &launches);
 
@@ -564,10 +636,12 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
     };
     PhaseVariant V;
     V.plain.resize(P.nphase);
+    V.tma.resize(P.nphase);
     V.spec.resize(P.nphase);
     for (int ph = 0; ph < P.nphase; ph++)
     {
-        std::vector<std::pair<dev::StepDesc, int>> pl, sp;
+        std::vector<std::pair<dev::StepDesc, int>> pl, tm, sp;
+        std::vector<const LevelDev *> tm_map;
         for (const int4 &e : P.entries[ph])
         {
             const mgpu_ctx *c = ctxs[e.x];
@@ -586,11 +660,38 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
             sd.o.snap_use = (mb && k > 0) ? 1 : 0;
             sd.spec_begin = ll.spec_begin;
             sd.spec_count = (int)ll.spec_count;
-            if (!ll.tile_list.empty()) pl.push_back({sd, (int)ll.tile_list.size()});
+            // x-interior tiles through the TMA pipeline (when the image uses it),
+            // the others with direct loads
+            const int nt = (int)ll.tile_list.size();
+            const int ni = c->lv[l].has_tmap ? ll.n_tiles_interior : 0;
+            if (ni > 0)
+            {
+                sd.tile_base = 0;
+                tm.push_back({sd, ni});
+                tm_map.push_back(&c->lv[l]);
+            }
+            if (nt > ni)
+            {
+                sd.tile_base = ni;
+                pl.push_back({sd, nt - ni});
+            }
+            sd.tile_base = 0;
             if (ll.spec_count) sp.push_back({sd, (int)((ll.spec_count + 127) / 128)});
         }
         V.plain[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(pl);
         V.spec[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(sp);
+        V.tma[ph] = pack_launches<dev::TmaLaunch, dev::StepDesc, dev::kMaxTmaDescs>(tm);
+        for (size_t k = 0; k < V.tma[ph].size(); k++)
+        {
+            dev::TmaLaunch &t = V.tma[ph][k];
+            for (int j = 0; j < t.ndesc; j++)
+            {
+                const LevelDev *ld = tm_map[k * dev::kMaxTmaDescs + j];
+                t.map[j] = ld->tmap;
+                t.om_map[j] = ld->om_map;
+            }
+            t.grid = std::min(t.start[t.ndesc], ctxs[0]->sm_count * 4);
+        }
     }
     std::vector<std::vector<std::pair<dev::PairDesc, int>>> wv(P.nwave);
     for (const int2 &pr : P.pairs)
@@ -626,17 +727,26 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
     return P.variants.emplace(key, std::move(V)).first->second;
 }
 
-// The launches of one phase: plain-cell blocks on `main`, special-cell blocks
-// forked onto `side` (their slot sets are disjoint under the AA ownership rule).
-void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::PhaseLaunch> &spec,
-                  const dev::PhaseArgs &a, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
-                  int64_t &launches)
+// The launches of one phase: plain cells on `main` (TMA tiles, direct-load
+// tiles), special cells forked onto `side` (their slot sets are disjoint
+// under the AA ownership rule).
+void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::TmaLaunch> &tma,
+                  const std::vector<dev::PhaseLaunch> &spec, const dev::PhaseArgs &a, cudaStream_t main,
+                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int64_t &launches)
 {
-    const bool both = !plain.empty() && !spec.empty();
+    const bool both = (!plain.empty() || !tma.empty()) && !spec.empty();
     if (both)
     {
         CK(cudaEventRecord(fork, main));
         CK(cudaStreamWaitEvent(side, fork, 0));
+    }
+    for (const auto &t0 : tma)
+    {
+        dev::TmaLaunch t = t0;
+        t.a = a;
+        dev::k_phase_plain_tma<<<(unsigned)t.grid, 256, 0, main>>>(t);
+        CK(cudaGetLastError());
+        launches++;
     }
     for (const auto &l0 : plain)
     {
@@ -673,7 +783,7 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     PhaseVariant &V = plan_variant(P, ctxs, 0);
     const dev::PhaseArgs none{0, 0, 0};
     for (int ph = 0; ph < P.nphase; ph++)
-        launch_phase(V.plain[ph], V.spec[ph], ph == 0 ? a : none, main, side, fork, join, launches);
+        launch_phase(V.plain[ph], V.tma[ph], V.spec[ph], ph == 0 ? a : none, main, side, fork, join, launches);
     for (int w = 0; w < P.nwave; w++)
         for (const auto &l : V.waves[w])
         {
@@ -722,6 +832,7 @@ void mgpu_default_params(mgpu_params *p)
     p->seed = 0;
     p->check_every = 1;
     p->edge_fine = 0;
+    p->plain_path = 1;
 }
 
 static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **out)
@@ -786,6 +897,12 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         d.f.alloc((size_t)ll.plane * 9, acct);
         d.f.zero(s);
         d.omega.upload(ll.omega, acct, s);
+        if (p->plain_path != 0 && !ctx->adsorption && ll.n_tiles_interior > 0)
+        {
+            encode_level_map(&d.tmap, d.f.p, ll);
+            encode_omega_map(&d.om_map, d.omega.p, ll);
+            d.has_tmap = true;
+        }
         d.spec.upload(ll.spec, acct, s);
         d.tiles.upload(ll.tile_list, acct, s);
         d.tile_mask.upload(ll.tile_mask, acct, s);
@@ -961,6 +1078,7 @@ int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
             }
         }
         CK(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
         if (steps_done) *steps_done = done;
         return MGPU_OK;
     });
@@ -1077,8 +1195,8 @@ int mgpu_step_level(mgpu_ctx *ctx, int level, int n)
         for (int i = 0; i < n; i++)
         {
             PhaseVariant &V = plan_variant(P, {ctx}, 0);
-            launch_phase(V.plain[0], V.spec[0], none, ctx->stream, ctx->side_stream, ctx->ev_fork, ctx->ev_join,
-                         ctx->launches);
+            launch_phase(V.plain[0], V.tma[0], V.spec[0], none, ctx->stream, ctx->side_stream, ctx->ev_fork,
+                         ctx->ev_join, ctx->launches);
             ctx->lv[l].steps++;
         }
         return MGPU_OK;
@@ -1101,6 +1219,7 @@ int mgpu_sync(mgpu_ctx *ctx)
     return guarded(ctx, [&]() {
         if (!ctx) throw std::invalid_argument("null context");
         CK(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
         return MGPU_OK;
     });
 }

@@ -37,6 +37,7 @@ class Params(C.Structure):
         ("seed", C.c_uint64),
         ("check_every", C.c_int),
         ("edge_fine", C.c_int),
+        ("plain_path", C.c_int),
     ]
 
 
