@@ -76,6 +76,9 @@ typedef struct mgpu_info
     double tau_mean;       /* mean tau_s over non-buffer cells (permeability viscosity) */
     int64_t device_bytes;  /* device memory held by the context */
     int64_t grid_undefined_cases; /* reference-undefined cases given a defined meaning */
+    int plain_path;        /* plain-cell path in use: 1 TMA pipeline, 0 direct loads */
+    int pad_;
+    double autotune_us[2]; /* plain_path -1: measured microseconds per coarse step, direct / TMA (else 0) */
 } mgpu_info;
 
 void mgpu_default_params(mgpu_params *p);

@@ -181,6 +181,7 @@ struct mgpu_ctx
     std::unique_ptr<PhasePlan> plan; // phase engine tables of this image
     std::vector<std::unique_ptr<PhasePlan>> level_plans; // single-level tables (mgpu_step_level)
     int sm_count = 1;
+    double autotune_us[2] = {0.0, 0.0}; // plain_path -1: direct / TMA microseconds per coarse step
     int64_t coarse_done = 0;     // coarse steps executed since creation
     int64_t ref_t = 0;           // reference lb->t
     std::vector<double> residuals;
@@ -798,6 +799,47 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     }
 }
 
+// plain_path -1: times both plain-cell paths over a few coarse steps from the
+// initial state, puts the state back and keeps the faster path.
+void autotune_plain_path(mgpu_ctx *ctx)
+{
+    bool any = false;
+    for (auto &l : ctx->lv) any |= l.has_tmap;
+    if (!any) return;
+    std::vector<bool> had;
+    for (auto &l : ctx->lv) had.push_back(l.has_tmap);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    checkpoint_save(ctx);
+    const int64_t launches0 = ctx->launches;
+    double us[2] = {0.0, 0.0};
+    for (int path = 0; path < 2; path++)
+    {
+        for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].has_tmap = path == 1 && had[l];
+        ctx->plan = build_plan({ctx}, -1);
+        for (int i = 0; i < 2; i++) coarse_step(ctx, false, false, 0);
+        const int n = 6;
+        CK(cudaEventRecord(e0, ctx->stream));
+        for (int i = 0; i < n; i++) coarse_step(ctx, false, false, 0);
+        CK(cudaEventRecord(e1, ctx->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        us[path] = ms * 1e3 / n;
+        checkpoint_restore(ctx);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaEventDestroy(e0));
+    CK(cudaEventDestroy(e1));
+    const bool tma = us[1] < us[0];
+    for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].has_tmap = tma && had[l];
+    ctx->plan = build_plan({ctx}, -1);
+    ctx->autotune_us[0] = us[0];
+    ctx->autotune_us[1] = us[1];
+    ctx->launches = launches0;
+}
+
 void check_supported(mgpu_ctx *ctx)
 {
     if (ctx->prm.simulation == MGPU_SIM_COUPLED)
@@ -968,6 +1010,7 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         launch_check(ctx.get());
     }
     CK(cudaStreamSynchronize(s));
+    if (p->plain_path < 0 && !ctx->adsorption) autotune_plain_path(ctx.get());
     *out = ctx.release();
     return MGPU_OK;
 }
@@ -1028,6 +1071,11 @@ int mgpu_get_info(const mgpu_ctx *ctx, mgpu_info *info)
     const GridDiagnostics &d = ctx->grid.diag;
     info->grid_undefined_cases =
         d.buffer_wall_links + d.fine_parent_missing_nbr + d.coarse_missing_child + d.fine_group_unmatched + d.pore_search_failed;
+    bool tma = false;
+    for (auto &l : ctx->lv) tma |= l.has_tmap;
+    info->plain_path = tma ? 1 : 0;
+    info->autotune_us[0] = ctx->autotune_us[0];
+    info->autotune_us[1] = ctx->autotune_us[1];
     return MGPU_OK;
 }
 

@@ -55,6 +55,9 @@ class Info(C.Structure):
         ("tau_mean", C.c_double),
         ("device_bytes", C.c_int64),
         ("grid_undefined_cases", C.c_int64),
+        ("plain_path", C.c_int),
+        ("pad_", C.c_int),
+        ("autotune_us", C.c_double * 2),
     ]
 
 
@@ -261,7 +264,8 @@ class Solver:
         self._h = h
         inf = Info()
         L.mgpu_get_info(h, C.byref(inf))
-        self.info = {f: getattr(inf, f) for f, _ in Info._fields_}
+        self.info = {f: getattr(inf, f) for f, _ in Info._fields_ if f != "pad_"}
+        self.info["autotune_us"] = tuple(self.info["autotune_us"])
         self.n = self.info["n"]
         self.n_cells = self.info["n_cells"]
 
