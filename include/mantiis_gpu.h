@@ -152,6 +152,11 @@ int mgpu_download_pixels(mgpu_ctx *ctx, double *rho, double *ux, double *uy, dou
  * nu = (tau_mean - 1/2) / 3, out[2] = total mass over pixels, out[3] = last residual. */
 int mgpu_observables(mgpu_ctx *ctx, double out[4]);
 
+/* Top-left pixel (x, y) and level of every reference cell, in reference
+ * cell order (Grid2D::gridIJ / gridLevel, include/grid.hpp:167-264); any
+ * pointer may be NULL. */
+int mgpu_cell_positions(const mgpu_ctx *ctx, int32_t *x, int32_t *y, int32_t *level);
+
 /* The quadtree image the grid was built from (n*n row-major, +cell number for
  * void leaves, -cell number for solid ones), as Grid2D::initialize writes it
  * to reconstructed.dat (include/grid.hpp:281-287). */

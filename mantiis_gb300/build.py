@@ -4,6 +4,8 @@ Outputs (git-ignored, rebuilt on each machine):
   mantiis_gb300/lib/libmantiis_gpu.so  C ABI of include/mantiis_gpu.h: host grid
                                        builder (C++) + sm_103a kernels (CUDA)
   mantiis_gb300/bin/mantiis            drop-in for the reference executable
+  mantiis_gb300/lib/libmantiis_cnn.so  C ABI of include/mantiis_cnn.h: the warm-start
+                                       network's kernels (CUDA)
 Object files go to _build/.  Everything is compiled for sm_103a only.
 """
 import concurrent.futures as cf
@@ -18,6 +20,8 @@ CSRC = PKG / "csrc"
 OBJ = ROOT / "_build"
 LIB = PKG / "lib" / "libmantiis_gpu.so"
 BIN = PKG / "bin" / "mantiis"
+CNN_LIB = PKG / "lib" / "libmantiis_cnn.so"
+CNN_SOURCES = ["cnn/cnn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = [
@@ -39,7 +43,8 @@ def _nvcc():
 
 
 def _headers():
-    return [p for p in CSRC.rglob("*") if p.suffix in (".h", ".hpp", ".cuh")] + [ROOT / "include" / "mantiis_gpu.h"]
+    return [p for p in CSRC.rglob("*") if p.suffix in (".h", ".hpp", ".cuh")] + [ROOT / "include" / "mantiis_gpu.h",
+                                                                               ROOT / "include" / "mantiis_cnn.h"]
 
 
 def _stale(target: Path, deps):
@@ -78,11 +83,20 @@ def build(verbose=False, jobs=None):
         objs.append(o)
         if _stale(o, [s] + hdrs):
             steps.append([nvcc, "-std=c++17", *ARCH, "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-c", s, "-o", o])
+    cnn_objs = []
+    for src in CNN_SOURCES:
+        s = CSRC / src
+        o = OBJ / (src.replace("/", "_") + ".o")
+        cnn_objs.append(o)
+        if _stale(o, [s] + hdrs):
+            steps.append([nvcc, "-std=c++17", *ARCH, "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         for out in ex.map(lambda c: _run(c, verbose), steps):
             pass
     if steps or not LIB.exists() or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lpthread"], verbose)
+    if not CNN_LIB.exists() or _stale(CNN_LIB, cnn_objs):
+        _run([nvcc, *ARCH, "-shared", "-o", CNN_LIB, *cnn_objs], verbose)
     app = [CSRC / a for a in APP_SOURCES]
     if _stale(BIN, app + hdrs + [LIB]):
         _run(["g++", "-std=c++17", "-O2", "-Wall", *app, "-o", BIN, "-L", LIB.parent, "-lmantiis_gpu",

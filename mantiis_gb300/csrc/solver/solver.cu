@@ -1367,6 +1367,15 @@ int mgpu_observables(mgpu_ctx *ctx, double out[4])
     });
 }
 
+int mgpu_cell_positions(const mgpu_ctx *ctx, int32_t *x, int32_t *y, int32_t *level)
+{
+    if (!ctx) return fail(nullptr, MGPU_E_ARG, "null context");
+    if (x) std::copy(ctx->grid.x.begin(), ctx->grid.x.end(), x);
+    if (y) std::copy(ctx->grid.y.begin(), ctx->grid.y.end(), y);
+    if (level) std::copy(ctx->grid.level.begin(), ctx->grid.level.end(), level);
+    return MGPU_OK;
+}
+
 int mgpu_reconstructed(const mgpu_ctx *ctx, int64_t *out)
 {
     if (!ctx || !out) return fail(nullptr, MGPU_E_ARG, "null argument");

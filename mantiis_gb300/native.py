@@ -93,6 +93,7 @@ SIGNATURES = {
     "mgpu_download_pixels": (C.c_int, [P, P, P, P, P]),
     "mgpu_observables": (C.c_int, [P, F64P]),
     "mgpu_reconstructed": (C.c_int, [P, I64P]),
+    "mgpu_cell_positions": (C.c_int, [P, P, P, P]),
     "mgpu_set_equilibrium": (C.c_int, [P, F64P, F64P, F64P]),
     "mgpu_set_equilibrium_noalloc": (C.c_int, [P, F64P, F64P, F64P]),
     "mgpu_set_stream": (C.c_int, [P, P]),
@@ -334,6 +335,12 @@ class Solver:
         out = np.zeros(4)
         self._check(lib().mgpu_observables(self._h, out))
         return dict(mean_ux=out[0], permeability=out[1], mass=out[2], residual=out[3])
+
+    def cell_positions(self):
+        """Top-left pixel (x, y) and level of every cell, in cell order."""
+        x, y, lv = (np.zeros(self.n_cells, np.int32) for _ in range(3))
+        self._check(lib().mgpu_cell_positions(self._h, _ptr(x), _ptr(y), _ptr(lv)))
+        return x, y, lv
 
     def reconstructed(self):
         out = np.zeros(self.n * self.n, np.int64)

@@ -1,0 +1,389 @@
+"""Learned warm start for the steady transport state.
+
+An encoder-decoder CNN (4 pooling levels down, 4 upsampling levels up, widths
+32-64-128-256 with a 256-wide bottleneck, skip connections by addition) maps a
+pore image and its log Knudsen-number map to the steady velocity and density
+fields.  Its forward and backward passes run on the kernels of
+libmantiis_cnn.so (include/mantiis_cnn.h): 3x3 convolutions with BF16 weights
+and FP32 accumulation, pooling, upsampling, ReLU, a masked squared-error loss
+and Adam.  PyTorch only holds the device buffers.
+
+The prediction only initialises the lattice Boltzmann state (f = f_eq of the
+predicted fields, with the mass of the solver's own start); the solver then
+iterates to its own convergence criterion, so every reported field and
+permeability is the solver's converged result.  The reference has no
+counterpart: it always starts from rest (include/coreLB.hpp:381-417).
+
+Targets are scaled so that they do not depend on the body force or the mean
+viscosity: u * nu_mean / F_body and (rho - rho_in) * nu_mean / F_body, each
+divided by a dataset-wide constant (UNet.scale).
+"""
+import ctypes as C
+import time
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libmantiis_cnn.so"
+_cnn = None
+
+_P = C.c_void_p
+_SIG = {
+    "cnn_conv3x3_forward": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_conv3x3_backward_data": [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_conv3x3_backward_weight": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_relu_backward": [_P, _P, C.c_int64, _P],
+    "cnn_avgpool2_forward": [_P, _P, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_avgpool2_backward": [_P, _P, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_upsample2_forward": [_P, _P, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_upsample2_backward": [_P, _P, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_add": [_P, _P, C.c_int64, _P],
+    "cnn_mse": [_P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _P],
+    "cnn_adam": [_P, _P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, _P],
+    "cnn_to_bf16": [_P, _P, C.c_int64, _P],
+}
+
+
+def cnn_lib():
+    """Loads libmantiis_cnn.so (raises if it has not been built)."""
+    global _cnn
+    if _cnn is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with mantiis_gb300.build.build() first")
+        L = C.CDLL(str(LIB_PATH))
+        for name, args in _SIG.items():
+            fn = getattr(L, name)
+            fn.restype = C.c_int
+            fn.argtypes = args
+        _cnn = L
+    return _cnn
+
+
+def _ptr(t):
+    """Device address of a contiguous CUDA tensor (the kernels take FP32 data or BF16 bits)."""
+    if t is None:
+        return None
+    import torch
+
+    if not (t.is_cuda and t.is_contiguous() and t.dtype in (torch.float32, torch.int16)):
+        raise TypeError(f"expected a contiguous float32 / int16 CUDA tensor, got {t.dtype} {tuple(t.shape)}")
+    return C.c_void_p(t.data_ptr())
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"{what} failed with status {rc}")
+
+
+def _stream():
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Conv3x3:
+    """3x3 convolution: FP32 master weights (for Adam), BF16 copy (for the kernels)."""
+
+    def __init__(self, cin, cout, rng, scale=None):
+        import torch
+
+        self.cin, self.cout = cin, cout
+        std = scale if scale is not None else np.sqrt(2.0 / (9 * cin))
+        w = (rng.standard_normal((cout, cin, 3, 3)) * std).astype(np.float32)
+        self.w = torch.tensor(w, dtype=torch.float32, device="cuda")
+        self.b = torch.zeros(cout, dtype=torch.float32, device="cuda")
+        self.w16 = torch.empty(w.size, dtype=torch.int16, device="cuda")
+        self.dw = torch.zeros_like(self.w)
+        self.db = torch.zeros_like(self.b)
+        self.state = [torch.zeros_like(self.w), torch.zeros_like(self.w), torch.zeros_like(self.b),
+                      torch.zeros_like(self.b)]
+        self.sync_bf16()
+
+    def sync_bf16(self):
+        _check(cnn_lib().cnn_to_bf16(_ptr(self.w), _ptr(self.w16), self.w.numel(), _stream()), "to_bf16")
+
+    def forward(self, x, relu):
+        import torch
+
+        n, _, h, w = x.shape
+        y = torch.empty((n, self.cout, h, w), dtype=torch.float32, device="cuda")
+        _check(cnn_lib().cnn_conv3x3_forward(_ptr(x), _ptr(self.w16), _ptr(self.b), _ptr(y), n, self.cin, self.cout,
+                                             h, w, 1 if relu else 0, _stream()), "conv forward")
+        return y
+
+    def backward(self, x, dy, need_dx=True):
+        """Accumulates dw, db from the layer input x and output gradient dy; returns dx."""
+        import torch
+
+        n, _, h, w = x.shape
+        L = cnn_lib()
+        _check(L.cnn_conv3x3_backward_weight(_ptr(x), _ptr(dy), _ptr(self.dw), _ptr(self.db), n, self.cin, self.cout,
+                                             h, w, _stream()), "conv weight gradient")
+        if not need_dx:
+            return None
+        dx = torch.empty_like(x)
+        _check(L.cnn_conv3x3_backward_data(_ptr(dy), _ptr(self.w16), _ptr(dx), n, self.cin, self.cout, h, w,
+                                           _stream()), "conv data gradient")
+        return dx
+
+    def zero_grad(self):
+        self.dw.zero_()
+        self.db.zero_()
+
+    def adam(self, lr, step, b1=0.9, b2=0.999, eps=1e-8):
+        L = cnn_lib()
+        _check(L.cnn_adam(_ptr(self.w), _ptr(self.dw), _ptr(self.state[0]), _ptr(self.state[1]), _ptr(self.w16),
+                          self.w.numel(), lr, b1, b2, eps, step, _stream()), "adam")
+        _check(L.cnn_adam(_ptr(self.b), _ptr(self.db), _ptr(self.state[2]), _ptr(self.state[3]), None,
+                          self.b.numel(), lr, b1, b2, eps, step, _stream()), "adam")
+
+
+def _relu_bw(dy, y):
+    _check(cnn_lib().cnn_relu_backward(_ptr(dy), _ptr(y), dy.numel(), _stream()), "relu backward")
+    return dy
+
+
+def _pool(x):
+    import torch
+
+    n, c, h, w = x.shape
+    y = torch.empty((n, c, h // 2, w // 2), dtype=torch.float32, device="cuda")
+    _check(cnn_lib().cnn_avgpool2_forward(_ptr(x), _ptr(y), n * c, h, w, _stream()), "pool")
+    return y
+
+
+def _pool_bw(dy, shape):
+    import torch
+
+    n, c, h, w = shape
+    dx = torch.empty(shape, dtype=torch.float32, device="cuda")
+    _check(cnn_lib().cnn_avgpool2_backward(_ptr(dy), _ptr(dx), n * c, h, w, _stream()), "pool backward")
+    return dx
+
+
+def _up(x):
+    import torch
+
+    n, c, h, w = x.shape
+    y = torch.empty((n, c, 2 * h, 2 * w), dtype=torch.float32, device="cuda")
+    _check(cnn_lib().cnn_upsample2_forward(_ptr(x), _ptr(y), n * c, h, w, _stream()), "upsample")
+    return y
+
+
+def _up_bw(dy):
+    import torch
+
+    n, c, h2, w2 = dy.shape
+    dx = torch.empty((n, c, h2 // 2, w2 // 2), dtype=torch.float32, device="cuda")
+    _check(cnn_lib().cnn_upsample2_backward(_ptr(dy), _ptr(dx), n * c, h2 // 2, w2 // 2, _stream()),
+           "upsample backward")
+    return dx
+
+
+def _add(y, x):
+    _check(cnn_lib().cnn_add(_ptr(y), _ptr(x), y.numel(), _stream()), "add")
+    return y
+
+
+class UNet:
+    """Encoder-decoder of widths w0..w3 and bottleneck w4; input 2 channels
+    (pore, scaled log Kn), output 3 channels (scaled u_x, u_y, rho - rho_in).
+    Image sides must be multiples of 16."""
+
+    def __init__(self, widths=(32, 64, 128, 256, 256), cin=2, cout=3, seed=0):
+        rng = np.random.default_rng(seed)
+        w = widths
+        self.widths = tuple(widths)
+        self.enc0a = Conv3x3(cin, w[0], rng)
+        self.enc0b = Conv3x3(w[0], w[0], rng)
+        self.enc = [Conv3x3(w[i - 1], w[i], rng) for i in range(1, 5)]  # after pooling, levels 1..4
+        self.dec = [Conv3x3(w[i + 1], w[i], rng) for i in range(3, -1, -1)]  # after upsampling, levels 3..0
+        self.out = Conv3x3(w[0], cout, rng, scale=np.sqrt(1.0 / (9 * w[0])))
+        self.step = 0
+        self.scale = np.ones(3)  # target scaling (set from the training data)
+
+    def layers(self):
+        return [self.enc0a, self.enc0b, *self.enc, *self.dec, self.out]
+
+    def forward(self, x, keep=False):
+        a = {"x": x}
+        a["a0"] = self.enc0a.forward(x, True)
+        e = [self.enc0b.forward(a["a0"], True)]
+        p = [None]
+        for i in range(1, 5):
+            p.append(_pool(e[i - 1]))
+            e.append(self.enc[i - 1].forward(p[i], True))
+        d = {4: e[4]}
+        u, c = {}, {}
+        for k, i in enumerate(range(3, -1, -1)):
+            u[i] = _up(d[i + 1])
+            c[i] = self.dec[k].forward(u[i], True)
+            d[i] = _add(c[i].clone(), e[i])
+        y = self.out.forward(d[0], False)
+        if keep:
+            a.update(e=e, p=p, u=u, c=c, d=d)
+            self._acts = a
+        return y
+
+    def backward(self, dy):
+        a = self._acts
+        e, p, u, c, d = a["e"], a["p"], a["u"], a["c"], a["d"]
+        dd = self.out.backward(d[0], dy)
+        de = {}
+        for i in range(0, 4):
+            # d[i] = c[i] + e[i]: the gradient reaches the skip and the decoder conv
+            de[i] = dd.clone()
+            dc = _relu_bw(dd, c[i])
+            du = self.dec[3 - i].backward(u[i], dc)
+            dd = _up_bw(du)  # gradient of d[i + 1]
+        de[4] = dd
+        for i in range(4, 0, -1):
+            g = _relu_bw(de[i], e[i])
+            dp = self.enc[i - 1].backward(p[i], g)
+            _add(de[i - 1], _pool_bw(dp, tuple(e[i - 1].shape)))
+        g = _relu_bw(de[0], e[0])
+        da0 = self.enc0b.backward(a["a0"], g)
+        g = _relu_bw(da0, a["a0"])
+        self.enc0a.backward(a["x"], g, need_dx=False)
+
+    def zero_grad(self):
+        for l in self.layers():
+            l.zero_grad()
+
+    def adam(self, lr):
+        self.step += 1
+        for l in self.layers():
+            l.adam(lr, self.step)
+
+
+def masked_loss(pred, target, mask):
+    """Mean squared error over fluid pixels and channels; returns (loss, dpred)."""
+    import torch
+
+    n, ch, h, w = pred.shape
+    norm = float(mask.sum().item()) * ch
+    dp = torch.empty_like(pred)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    _check(cnn_lib().cnn_mse(_ptr(pred), _ptr(target), _ptr(mask), _ptr(dp), _ptr(loss), n, ch, h, w,
+                             max(norm, 1.0), _stream()), "loss")
+    return loss, dp
+
+
+# ---- data: scaled inputs and targets, the solver's steady fields
+
+
+def network_input(pore, kn):
+    """2 x n x n: the void mask and log10(Kn) / 2 on void pixels."""
+    void = (pore == 1).astype(np.float32)
+    lk = np.where(pore == 1, np.log10(np.maximum(kn, 1e-12)) / 2.0, 0.0).astype(np.float32)
+    return np.stack([void, lk])
+
+
+def field_scale(solver):
+    """nu_mean / F_body of a solver: u * scale does not depend on the forcing."""
+    nu = (solver.info["tau_mean"] - 0.5) / 3.0
+    return nu / solver.params.fbody
+
+
+def steady_targets(solver):
+    """3 x n x n targets from a solver's current fields (before the dataset constant)."""
+    px = solver.pixels()
+    s = field_scale(solver)
+    void = px["rho"] != 0
+    drho = np.where(void, px["rho"] - solver.info["rho_in"], 0.0)
+    return np.stack([px["ux"] * s, px["uy"] * s, drho * s]).astype(np.float32)
+
+
+def run_to_steady(solver, chunk=1000, tol=1e-6, max_steps=200000):
+    """Advances in chunks until the permeability changes by less than tol
+    (relative) over one chunk.  Returns (steps, seconds spent stepping, the
+    host waiting for each chunk, permeability)."""
+    steps, secs = 0, 0.0
+    k_old = solver.observables()["permeability"]
+    while steps < max_steps:
+        t0 = time.perf_counter()
+        solver.advance_graph(chunk)
+        solver.sync()
+        secs += time.perf_counter() - t0
+        steps += chunk
+        k = solver.observables()["permeability"]
+        if k != 0 and abs(k - k_old) <= tol * abs(k):
+            return steps, secs, k
+        k_old = k
+    return steps, secs, k_old
+
+
+def run_batch_to_steady(batch, chunk=1000, tol=1e-6, max_steps=200000):
+    """run_to_steady for a batch: all images advance together until each one's
+    permeability has settled (settled images keep stepping).  Returns per image
+    the step count at which it settled (max_steps if never) and the permeabilities."""
+    k_old = np.array([o["permeability"] for o in batch.observables()])
+    n = len(k_old)
+    done = np.zeros(n, bool)
+    steps_at = np.full(n, max_steps)
+    steps = 0
+    while steps < max_steps and not done.all():
+        batch.advance(chunk)
+        batch.sync()
+        steps += chunk
+        k = np.array([o["permeability"] for o in batch.observables()])
+        newly = (~done) & np.isfinite(k) & (k != 0) & (np.abs(k - k_old) <= tol * np.abs(k))
+        steps_at[newly] = steps
+        done |= newly
+        k_old = k
+    return steps_at, k_old
+
+
+def predict(net, pore, kn):
+    """Network prediction (3 x n x n, in target units)."""
+    import torch
+
+    x = torch.tensor(network_input(pore, kn)[None], dtype=torch.float32, device="cuda")
+    y = net.forward(x).cpu().numpy()[0]
+    return y * net.scale[:, None, None]
+
+
+def warm_start(solver, net, pore, kn):
+    """Sets the solver's state to f_eq of the predicted fields at each cell's
+    top-left pixel.  The density is shifted so that the mass equals that of the
+    solver's own start (rho_in everywhere): a closed x-periodic system settles
+    to the steady state of its mass."""
+    y = predict(net, pore, kn)
+    s = field_scale(solver)
+    cx, cy, lv = solver.cell_positions()
+    ux = y[0][cy, cx] / s
+    uy = y[1][cy, cx] / s
+    drho = y[2][cy, cx] / s
+    area = 4.0 ** (lv - 1)
+    drho = drho - (drho * area).sum() / area.sum()
+    solver.set_equilibrium(solver.info["rho_in"] + drho, ux, uy)
+
+
+def train(net, inputs, targets, masks, epochs=20, batch=8, lr=1e-3, seed=0, log=None):
+    """Adam on the masked squared error; inputs / targets / masks are arrays
+    (N x 2 x n x n, N x 3 x n x n, N x n x n) of scaled data.  Returns the
+    mean loss of each epoch."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    X = torch.tensor(np.asarray(inputs, np.float32), device="cuda")
+    Y = torch.tensor(np.asarray(targets, np.float32), device="cuda")
+    M = torch.tensor(np.asarray(masks, np.float32), device="cuda")
+    history = []
+    t0 = time.perf_counter()
+    for ep in range(epochs):
+        order = rng.permutation(len(X))
+        tot = 0.0
+        for b0 in range(0, len(order), batch):
+            idx = torch.tensor(order[b0:b0 + batch], device="cuda")
+            x, y, m = X[idx].contiguous(), Y[idx].contiguous(), M[idx].contiguous()
+            net.zero_grad()
+            p = net.forward(x, keep=True)
+            loss, dp = masked_loss(p, y, m)
+            net.backward(dp)
+            net.adam(lr)
+            tot += float(loss.item()) * len(idx)
+        history.append(tot / len(order))
+        if log:
+            log(f"epoch {ep + 1}: loss {history[-1]:.4e} ({time.perf_counter() - t0:.1f} s)")
+    return history

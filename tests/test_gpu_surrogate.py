@@ -1,0 +1,64 @@
+"""The warm-start network's GPU kernels (libmantiis_cnn.so) against the FP64
+oracle (oracle/cnn_oracle.py): forward output, loss and every layer's weight
+and bias gradients, on a narrow network so that the oracle runs in seconds;
+and one Adam step with its BF16 copy."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_to_float(t16):
+    u = t16.cpu().numpy().view(np.uint16).astype(np.uint32) << 16
+    return u.view(np.float32).astype(np.float64)
+
+
+def test_network_gradients_match_oracle():
+    import torch
+
+    from mantiis_gb300 import surrogate as S
+    from oracle import cnn_oracle as co
+
+    net = S.UNet(widths=(8, 8, 16, 16, 16), seed=3)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((2, 2, 32, 32)).astype(np.float32)
+    t = rng.standard_normal((2, 3, 32, 32)).astype(np.float32)
+    mask = (rng.random((2, 32, 32)) > 0.3).astype(np.float32)
+    X, T, M = (torch.tensor(a, device="cuda") for a in (x, t, mask))
+    net.zero_grad()
+    p = net.forward(X, keep=True)
+    loss, dp = S.masked_loss(p, T, M)
+    net.backward(dp)
+    torch.cuda.synchronize()
+    params = [(bf16_to_float(l.w16).reshape(l.w.shape), l.b.cpu().numpy()) for l in net.layers()]
+    ref = co.Net(params)
+    yref = ref.forward(x.astype(np.float64))
+    lref, dref = co.masked_loss(yref, t, mask)
+    grads = ref.backward(dref)
+    # FP32 activations against FP64: relative bounds
+    e_y = np.abs(p.cpu().numpy() - yref).max() / np.abs(yref).max()
+    assert e_y < 1e-5
+    assert abs(float(loss.item()) - lref) < 1e-5 * lref
+    for l, (gw, gb) in zip(net.layers(), grads):
+        e_w = np.abs(l.dw.cpu().numpy() - gw).max() / max(np.abs(gw).max(), 1e-30)
+        e_b = np.abs(l.db.cpu().numpy() - gb).max() / max(np.abs(gb).max(), 1e-30)
+        assert e_w < 1e-4 and e_b < 1e-4, (e_w, e_b)
+
+
+def test_adam_step_and_bf16_copy():
+    import torch
+
+    from mantiis_gb300 import surrogate as S
+
+    rng = np.random.default_rng(1)
+    layer = S.Conv3x3(4, 4, rng)
+    w0 = layer.w.cpu().numpy().copy()
+    g = rng.standard_normal(w0.shape).astype(np.float32)
+    layer.dw.copy_(torch.tensor(g, device="cuda"))
+    layer.adam(1e-2, 1)
+    torch.cuda.synchronize()
+    # first Adam step: w - lr * g / (|g| + eps)
+    expect = w0 - 1e-2 * g / (np.abs(g) + 1e-8)
+    assert np.abs(layer.w.cpu().numpy() - expect).max() < 1e-6
+    w16 = bf16_to_float(layer.w16).reshape(w0.shape)
+    assert np.abs(w16 - layer.w.cpu().numpy()).max() <= np.abs(layer.w.cpu().numpy()).max() * 2 ** -8
