@@ -15,8 +15,10 @@ permeability is the solver's converged result.  The reference has no
 counterpart: it always starts from rest (include/coreLB.hpp:381-417).
 
 Targets are scaled so that they do not depend on the body force or the mean
-viscosity: u * nu_mean / F_body and (rho - rho_in) * nu_mean / F_body, each
-divided by a dataset-wide constant (UNet.scale).
+viscosity: u * nu_mean / F_body and (rho - rho_in) * nu_mean / F_body.  Pore
+velocities are heavy-tailed (throats carry orders of magnitude more than dead
+ends), so the network learns asinh(target / scale) with a per-channel scale
+(UNet.scale, the median magnitude of the training targets).
 """
 import ctypes as C
 import time
@@ -334,13 +336,22 @@ def run_batch_to_steady(batch, chunk=1000, tol=1e-6, max_steps=200000):
     return steps_at, k_old
 
 
+def target_scale(targets, masks):
+    """Per-channel scale of the encoding: median |target| over fluid pixels."""
+    return np.array([np.median(np.abs(targets[:, c][masks > 0])) + 1e-30 for c in range(targets.shape[1])])
+
+
+def encode(targets, scale):
+    return np.arcsinh(targets / scale[None, :, None, None]).astype(np.float32)
+
+
 def predict(net, pore, kn):
     """Network prediction (3 x n x n, in target units)."""
     import torch
 
     x = torch.tensor(network_input(pore, kn)[None], dtype=torch.float32, device="cuda")
-    y = net.forward(x).cpu().numpy()[0]
-    return y * net.scale[:, None, None]
+    y = net.forward(x).cpu().numpy()[0].astype(np.float64)
+    return np.sinh(y) * net.scale[:, None, None]
 
 
 def warm_start(solver, net, pore, kn):
