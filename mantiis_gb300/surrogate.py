@@ -398,3 +398,108 @@ def train(net, inputs, targets, masks, epochs=20, batch=8, lr=1e-3, seed=0, log=
         if log:
             log(f"epoch {ep + 1}: loss {history[-1]:.4e} ({time.perf_counter() - t0:.1f} s)")
     return history
+
+
+# ---- end-to-end: data from the batched solver, training, warm vs cold
+
+
+def synthetic_image(n, seed, porosity, kn_mean):
+    """Seeded disk image (void x-edge columns, see MGPU_DISKS_OPEN_X_EDGES) with
+    its local pore size, Kn map and the dx that gives the drawn mean Kn."""
+    from .native import generate_disks, pore_properties, units
+
+    pore = generate_disks(n, max(2, n // 64), max(4, n // 16), porosity, seed, open_x_edges=True)
+    H, ku = pore_properties(pore, 1.0, 1.0)
+    void = pore == 1
+    mfp = units()["mfp"]
+    dx = mfp * ku[void].mean() / kn_mean
+    return dict(pore=pore, kn=np.where(void, ku * mfp / dx, 0.0), locpore=H, dx=float(dx))
+
+
+def make_dataset(n, count, seed0=1000, chunk=500, tol=1e-6, max_steps=100000, log=None):
+    """Steady single-block fields of `count` seeded n x n images (porosity
+    U[0.5, 0.7], mean Kn log-uniform in [0.05, 1]), all stepped as one batch.
+    Images that do not settle are left out.  Returns X, Y (unencoded), M."""
+    from .native import Batch, Solver, default_params
+
+    rng = np.random.default_rng(seed0)
+    imgs = [synthetic_image(n, seed0 + i, rng.uniform(0.5, 0.7), float(np.exp(rng.uniform(np.log(0.05), 0.0))))
+            for i in range(count)]
+    sol = [Solver(d["pore"], d["kn"], d["locpore"], default_params(dx=d["dx"])) for d in imgs]
+    b = Batch(sol)
+    t0 = time.perf_counter()
+    steps, _ = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
+    X = np.stack([network_input(d["pore"], d["kn"]) for d in imgs])
+    Y = np.stack([steady_targets(s) for s in sol])
+    M = np.stack([(d["pore"] == 1) for d in imgs]).astype(np.float32)
+    good = np.isfinite(Y).all(axis=(1, 2, 3)) & (steps < max_steps)
+    if log:
+        log(f"data: {count} images {n}^2 settled in {int(steps[good].max()) if good.any() else 0} steps "
+            f"({time.perf_counter() - t0:.1f} s), kept {int(good.sum())}")
+    b.close()
+    for s in sol:
+        s.close()
+    return X[good], Y[good], M[good]
+
+
+def evaluate(net, n, count, seed0=90000, chunk=500, tol=1e-6, max_steps=200000, log=None):
+    """Cold start (rest) against warm start (network prediction) on held-out
+    images: steps and seconds to the permeability criterion, and the relative
+    difference of the two converged permeabilities."""
+    from .native import Solver, default_params
+
+    out = []
+    for i in range(count):
+        d = synthetic_image(n, seed0 + i, 0.6, 0.05 + 0.95 * i / max(1, count - 1))
+        p = default_params(dx=d["dx"])
+        cold = Solver(d["pore"], d["kn"], d["locpore"], p)
+        sc, tc, kc = run_to_steady(cold, chunk, tol, max_steps)
+        warm = Solver(d["pore"], d["kn"], d["locpore"], p)
+        t0 = time.perf_counter()
+        warm_start(warm, net, d["pore"], d["kn"])
+        t_pred = time.perf_counter() - t0
+        sw, tw, kw = run_to_steady(warm, chunk, tol, max_steps)
+        tgt = steady_targets(cold)
+        pred = predict(net, d["pore"], d["kn"])
+        void = d["pore"] == 1
+        err = float(np.abs(pred[0] - tgt[0])[void].mean() / max(np.abs(tgt[0])[void].mean(), 1e-30))
+        out.append(dict(cold_steps=int(sc), warm_steps=int(sw), cold_s=tc, warm_s=tw + t_pred,
+                        permeability_rel_diff=abs(kw - kc) / abs(kc), prediction_rel_err=err))
+        if log:
+            log(str(out[-1]))
+        cold.close()
+        warm.close()
+    return out
+
+
+def main(argv=None):
+    """python -m mantiis_gb300.surrogate --size 128 --train 512 --epochs 300 --eval 8
+    Trains the network on solver-generated steady fields and prints a JSON
+    report of the warm start against the cold start."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--train", type=int, default=512)
+    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--eval", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=5e-4)
+    a = ap.parse_args(argv)
+    log = lambda m: print(m, flush=True)  # noqa: E731
+    X, Y, M = make_dataset(a.size, a.train, log=log)
+    net = UNet(seed=1)
+    net.scale = target_scale(Y, M)
+    t0 = time.perf_counter()
+    hist = train(net, X, encode(Y, net.scale), M, epochs=a.epochs, lr=a.lr)
+    t_train = time.perf_counter() - t0
+    res = evaluate(net, a.size, a.eval, log=log)
+    cold = sum(r["cold_steps"] for r in res)
+    warm = sum(r["warm_steps"] for r in res)
+    print(json.dumps(dict(size=a.size, train_images=len(X), epochs=a.epochs, train_seconds=t_train,
+                          final_loss=hist[-1], cold_steps=cold, warm_steps=warm,
+                          step_ratio=cold / max(warm, 1), cases=res)))
+
+
+if __name__ == "__main__":
+    main()

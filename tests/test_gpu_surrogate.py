@@ -62,3 +62,24 @@ def test_adam_step_and_bf16_copy():
     assert np.abs(layer.w.cpu().numpy() - expect).max() < 1e-6
     w16 = bf16_to_float(layer.w16).reshape(w0.shape)
     assert np.abs(w16 - layer.w.cpu().numpy()).max() <= np.abs(layer.w.cpu().numpy()).max() * 2 ** -8
+
+
+def test_train_and_warm_start_small():
+    # the whole loop on a small case: solver-made training data, training on
+    # the GPU kernels, then the warm-started solver converges to the cold
+    # start's permeability; the step counts of both are recorded
+    from mantiis_gb300 import surrogate as S
+    from test_gpu_transport import record
+
+    X, Y, M = S.make_dataset(64, 32, chunk=250, tol=1e-6, max_steps=20000)
+    assert len(X) >= 24
+    net = S.UNet(widths=(16, 32, 64, 64, 64), seed=2)
+    net.scale = S.target_scale(Y, M)
+    hist = S.train(net, X, S.encode(Y, net.scale), M, epochs=150, batch=8, lr=2e-3)
+    assert min(hist[-10:]) < 0.25 * hist[0]
+    res = S.evaluate(net, 64, 2, chunk=250, tol=1e-7, max_steps=40000)
+    for i, r in enumerate(res):
+        assert r["warm_steps"] < 40000 and r["cold_steps"] < 40000
+        assert r["permeability_rel_diff"] < 1e-5
+        record(f"warm_start_64_{i}", cold_steps=r["cold_steps"], warm_steps=r["warm_steps"],
+               prediction_rel_err=r["prediction_rel_err"], k_rel=r["permeability_rel_diff"])
