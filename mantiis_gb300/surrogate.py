@@ -354,20 +354,24 @@ def predict(net, pore, kn):
     return np.sinh(y) * net.scale[:, None, None]
 
 
-def warm_start(solver, net, pore, kn):
-    """Sets the solver's state to f_eq of the predicted fields at each cell's
-    top-left pixel.  The density is shifted so that the mass equals that of the
-    solver's own start (rho_in everywhere): a closed x-periodic system settles
-    to the steady state of its mass."""
+def warm_start(solver, net, pore, kn, use_density=False):
+    """Sets the solver's state to f_eq of the predicted velocity at each cell's
+    top-left pixel, with the solver's own initial density rho_in.  The steady
+    density deviations are tiny, and an inexact predicted density field only
+    adds a slow pressure relaxation; use_density=True takes it anyway, shifted
+    to the mass of the solver's own start (a closed x-periodic system settles to
+    the steady state of its mass)."""
     y = predict(net, pore, kn)
     s = field_scale(solver)
     cx, cy, lv = solver.cell_positions()
     ux = y[0][cy, cx] / s
     uy = y[1][cy, cx] / s
-    drho = y[2][cy, cx] / s
-    area = 4.0 ** (lv - 1)
-    drho = drho - (drho * area).sum() / area.sum()
-    solver.set_equilibrium(solver.info["rho_in"] + drho, ux, uy)
+    rho = np.full(ux.shape, solver.info["rho_in"])
+    if use_density:
+        drho = y[2][cy, cx] / s
+        area = 4.0 ** (lv - 1)
+        rho = rho + drho - (drho * area).sum() / area.sum()
+    solver.set_equilibrium(rho, ux, uy)
 
 
 def train(net, inputs, targets, masks, epochs=20, batch=8, lr=1e-3, seed=0, log=None):

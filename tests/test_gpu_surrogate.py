@@ -77,9 +77,10 @@ def test_train_and_warm_start_small():
     net.scale = S.target_scale(Y, M)
     hist = S.train(net, X, S.encode(Y, net.scale), M, epochs=150, batch=8, lr=2e-3)
     assert min(hist[-10:]) < 0.25 * hist[0]
-    res = S.evaluate(net, 64, 2, chunk=250, tol=1e-7, max_steps=40000)
+    # a criterion tight enough that both runs settle within 1e-5 of each other
+    res = S.evaluate(net, 64, 2, chunk=250, tol=1e-8, max_steps=80000)
     for i, r in enumerate(res):
-        assert r["warm_steps"] < 40000 and r["cold_steps"] < 40000
+        assert r["warm_steps"] < 80000 and r["cold_steps"] < 80000
         assert r["permeability_rel_diff"] < 1e-5
         record(f"warm_start_64_{i}", cold_steps=r["cold_steps"], warm_steps=r["warm_steps"],
                prediction_rel_err=r["prediction_rel_err"], k_rel=r["permeability_rel_diff"])
