@@ -523,6 +523,49 @@ struct Oracle
         macroscopic();
         velocity_difference();
     }
+    // include/mantiisApp.hpp:267-284 (the coupling phase of the coupled run)
+    void coupled_step()
+    {
+        rho_old = rho;
+        density();
+        pseudo_potential();
+        forces();
+        velocity();
+        equilibrium();
+        collide_rmrt(1);
+        source();
+        ftemp = f;
+        zero_down(1);
+        stream(1);
+        srbb(1);
+        periodic(1);
+        velocity_difference(); // usq_old is never updated in this run: the ratio is 1
+    }
+    // the coupled run (include/mantiisApp.hpp:376-392): up to 100 adsorption
+    // steps without body force (ended early by the residual test), a reset of
+    // u, rho and f_eq, then coupling steps
+    int coupled_a = 0;
+    bool coupled_b = false;
+    void coupled_run_step()
+    {
+        if (coupled_b)
+        {
+            coupled_step();
+            return;
+        }
+        const double fb = p.fbody;
+        p.fbody = 0.0;
+        adsorption_step();
+        p.fbody = fb;
+        coupled_a++;
+        if (coupled_a >= 100 || diff < p.tol)
+        {
+            coupled_b = true;
+            std::fill(ux.begin(), ux.end(), 0.0);
+            std::fill(rho.begin(), rho.end(), p.rhoin);
+            std::fill(feq.begin(), feq.end(), 0.0);
+        }
+    }
     // include/mantiisApp.hpp:248-265
     void adsorption_step()
     {
@@ -618,6 +661,16 @@ int oracle_run(void *h, int n, int break_on_tol)
     int done = 0;
     for (int i = 0; i < n; i++)
     {
+        if (o->p.simulation == 2)
+        {
+            // the first phase ends on the residual test, the coupling phase runs on
+            const bool in_a = !o->coupled_b;
+            o->coupled_run_step();
+            done++;
+            if (!in_a && break_on_tol && o->diff < o->p.tol) break;
+            o->t++;
+            continue;
+        }
         if (o->p.simulation == 1) o->adsorption_step();
         else o->transport_step();
         done++;

@@ -47,7 +47,7 @@ typedef struct OracleGrid
 
 typedef struct OracleParams
 {
-    int simulation; /* 0 transport, 1 adsorption */
+    int simulation; /* 0 transport, 1 adsorption, 2 coupled */
     int collision;  /* 0 BGK, 1 MRT, 2 regularized MRT */
     int wall;       /* 0 BB, 1 MDBB, 2 SRBB */
     double fbody, rhoin, mfp, Cl, T_lu, a_alpha_lu;

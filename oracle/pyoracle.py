@@ -142,7 +142,7 @@ def for_grid(grid, sim="transport", dx=1e-9, T=300.0, P=2.0e6, fbody=1e-8, **kw)
     from mantiis_gb300 import units
 
     u = units(dx, T, P)
-    simulation = 1 if sim == "adsorption" else 0
+    simulation = {"transport": 0, "adsorption": 1, "coupled": 2}[sim]
     if simulation == 1:
         kw.setdefault("collision", 1)
         kw.setdefault("wall", 0)

@@ -154,7 +154,20 @@ def main():
             np.savez_compressed(HERE / f"refgrid_{name}.npz", img_pore=p, img_kn=kn, img_locpore=lp, **grid)
             np.savez_compressed(HERE / f"refstate_{name}.npz",
                                 **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
+    coupled_fixture(fx)
     print("fixtures written to", HERE)
+
+
+def coupled_fixture(fx):
+    """The reference's coupled run (include/mantiisApp.hpp:376-392) on the 64x64
+    test image, single block, dx = 12 nm: 100 adsorption steps without body
+    force, then coupling steps; states after 100, 101 and 130 steps."""
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "fx64"
+        write_col_major(f, fx["pore"], fx["kn"], fx["locpore"])
+        grid, states = run_ref(f, 64, 30, False, mode="coupled", dx=12e-9, dump_steps=(100, 101, 130))
+        np.savez_compressed(HERE / "refstate_coupled64.npz",
+                            **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
 
 
 if __name__ == "__main__":

@@ -56,3 +56,25 @@ def test_oracle_break_semantics(fixture64):
     assert (r[:29] > tol).all()
     o2 = for_grid(g, sim="transport", dx=1e-9, tol=tol)
     assert o2.run(100, break_on_tol=True) == 30
+
+
+def test_oracle_coupled_run_matches_reference_code(fixture64):
+    # refstate_coupled64.npz: the reference's own coupled run (oracle/_ref,
+    # tests/golden/make_golden.py); at step 100 the run resets u and rho, so
+    # only f is compared there
+    from mantiis_gb300 import HostGrid, default_params
+    from oracle.pyoracle import for_grid
+
+    st = load("refstate_coupled64.npz")
+    g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=12e-9))
+    o = for_grid(g, sim="coupled", dx=12e-9)
+    done = 0
+    for step in (100, 101, 130):
+        o.run(step - done, break_on_tol=True)
+        done = step
+        f = o.fields()
+        assert np.abs(f["f"] - st[f"f_{step}"]).max() < 1e-10
+        if step > 100:
+            assert np.abs(f["ux"] - st[f"ux_{step}"]).max() < 1e-10
+            assert np.abs(f["rho"] - st[f"rho_{step}"]).max() < 1e-10
+    assert np.allclose(o.residuals()[100:], 1.0)
