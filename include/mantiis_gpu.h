@@ -104,7 +104,11 @@ int mgpu_get_info(const mgpu_ctx *ctx, mgpu_info *info);
  * transport_simulation_loop / adsorption_simulation_loop
  * (include/mantiisApp.hpp:239-265), stopping after the first step whose
  * residual is below tol, exactly like the reference's break.  *steps_done
- * receives the number of steps executed in this call. */
+ * receives the number of steps executed in this call.  A coupled run
+ * (MGPU_SIM_COUPLED, include/mantiisApp.hpp:376-392) spends its first steps
+ * (100, or fewer if the residual test ends that phase) in the adsorption step
+ * without body force, then takes coupled_simulation_loop's step
+ * (include/mantiisApp.hpp:267-284); only a break in the coupling phase stops. */
 int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done);
 
 /* Runs exactly n_steps coarse steps with no residual and no break; the

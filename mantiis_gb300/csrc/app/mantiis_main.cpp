@@ -167,6 +167,13 @@ int main(int argc, char *argv[])
             hist.resize((size_t)cnt);
             mgpu_residuals(ctx, hist.data(), cnt, &cnt);
         };
+        const bool coupled = p.simulation == MGPU_SIM_COUPLED;
+        if (coupled)
+        {
+            // 100 adsorption steps come first (include/mantiisApp.hpp:376-392)
+            iters += 100;
+            std::cout << "======================= Adsorption ONLY for initial condition =======================\n";
+        }
         while (done_total < iters && !stopped)
         {
             // first step alone (its fields are dumped as ux_0 / uy_0), then in chunks
@@ -177,6 +184,7 @@ int main(int argc, char *argv[])
             residuals();
             for (size_t k = h0; k < hist.size(); k++)
             {
+                if (coupled && t == 100) std::cout << "======================= Coupling =======================\n";
                 if (t % st.verbose == 0)
                     std::cout << "Timestep: " << t << ", residual difference: " << hist[k] << "\n";
                 if (hist[k] < st.threshold)

@@ -64,6 +64,7 @@ struct Common
     float eos_a, eos_b, eos_T; // a_alpha_lu, b_lu, T_lu
     float g_ff, g_fs;
     int adsorption;       // Shan-Chen step (outputs come from the snapshot planes)
+    int inlet_outlet;     // apply the adsorption inlet / outlet values (not in the coupling phase)
     double *red;          // reduction accumulators
     unsigned int *err;    // device error word
 };
@@ -384,12 +385,12 @@ __device__ __forceinline__ void special_rules(const Common &C, const SpecialRec 
 #pragma unroll
         for (int q = 0; q < 9; q++) df[q] += k[q];
     }
-    if (flags & SF_INLET)
+    if ((flags & SF_INLET) && C.inlet_outlet)
     {
         df[1] = C.inlet_axis;
         df[5] = df[8] = C.inlet_diag;
     }
-    if (flags & SF_OUTLET)
+    if ((flags & SF_OUTLET) && C.inlet_outlet)
     {
         df[3] = C.inlet_axis;
         df[6] = df[7] = C.inlet_diag;

@@ -480,14 +480,15 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, C
 // (:694-742), Guo source term (:568-630), AA store.  Bounce-back walls, the
 // x-periodic links and the inlet/outlet overwrite (:859-865, 969-1009) are
 // applied when the populations are read in the next step.
-template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
+// The coupling phase of the coupled run (include/mantiisApp.hpp:267-284) takes
+// the same body with the regularized MRT, SRBB walls, no inlet / outlet and the
+// velocity residual (C.collision, C.wall, C.inlet_outlet; o.diff accumulates
+// sum |u| for both terms, as its |u| of the previous step is never stored).
+template <int P>
+__device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y,
+                                         double &r_diff, double &r_norm)
 {
-    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
-    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
-    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
-    if (x >= L.W || y >= L.H) return;
     const int64_t s = site_of(L, x, y);
-    if (L.omega[s] == 0.0f) return;
     float df[9];
     bool special;
     SpecialRec rec;
@@ -535,10 +536,17 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, 
         L.snap[L.plane + s] = ux;
         L.snap[2 * L.plane + s] = uy;
     }
+    if (o.diff)
+    {
+        const float un = sqrtf(ux * ux + uy * uy);
+        r_diff = (double)un;
+        r_norm = (double)un;
+    }
     float feq[9], fs[9];
     equilibrium(drho, rho, ux, uy, feq);
     const float tau_s = 1.0f / omega, tau_d = L.tau2[s];
-    collide_mrt(df, feq, tau_s, tau_d, fs);
+    if (C.collision == COLL_RMRT) collide_rmrt(df, feq, drho, rho, ux, uy, omega, fs);
+    else collide_mrt(df, feq, tau_s, tau_d, fs);
     add_source(fs, ux, uy, Fx, Fy, tau_s, tau_d);
     if (special && (rec.m1 & 0x1FFu))
     {
@@ -550,6 +558,16 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, 
             if ((quirk >> q) & 1u) side_now[rec.quirk_base + qi++] = fs[q];
     }
     store_post<P>(L, x, y, fs);
+}
+
+template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
+{
+    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
+    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
+    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
+    double r_diff = 0.0, r_norm = 0.0;
+    if (x < L.W && y < L.H && L.omega[site_of(L, x, y)] != 0.0f) ads_cell<P>(L, C, o, x, y, r_diff, r_norm);
+    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 
 // Reads the current state of every reference cell (no update): FP64 density,

@@ -174,6 +174,12 @@ struct mgpu_ctx
     DevBuf<unsigned int> errword;
     float rho0f = 0.f;
     bool adsorption = false; // Shan-Chen step body (include/mantiisApp.hpp:248-265)
+    // coupled run (include/mantiisApp.hpp:376-392): up to 100 adsorption steps
+    // without body force, then coupling steps (regularized MRT, SRBB walls)
+    bool coupled = false, coupled_b = false;
+    int coupled_a = 0;                   // adsorption-phase steps done
+    DevBuf<SpecialRec> specials_b;       // records with SRBB wall coefficients / constants
+    DevBuf<float> ktab_b;
 
     cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
     std::string graph_key;           // level parities the graph was captured at
@@ -195,6 +201,8 @@ struct mgpu_ctx
         std::vector<std::unique_ptr<DevBuf<float>>> unorm;
         std::vector<int64_t> steps;
         int64_t coarse_done = 0;
+        int coupled_a = 0;
+        bool coupled_b = false;
         bool valid = false;
     } ckpt;
 
@@ -213,7 +221,17 @@ struct mgpu_ctx
         C.wall = adsorption ? WALL_BB : prm.wall;
         C.collision = adsorption ? COLL_MRT : prm.collision;
         C.adsorption = adsorption ? 1 : 0;
+        C.inlet_outlet = 1;
         C.fbody = (float)prm.fbody;
+        if (coupled && !coupled_b) C.fbody = 0.0f; // the adsorption phase runs without body force
+        if (coupled && coupled_b)
+        {
+            C.wall = WALL_SRBB;
+            C.collision = COLL_RMRT;
+            C.inlet_outlet = 0;
+            C.specials = specials_b.p;
+            C.ktab = ktab_b.p;
+        }
         C.psi_form = prm.psi_form;
         C.psi_rho0 = (float)prm.rho_psi;
         C.eos_a = (float)units.a_alpha_lu;
@@ -414,21 +432,26 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         dev::StepOpt o{};
         o.parity = (int)(ctx->lv[0].steps & 1);
         o.direct = ctx->lv[0].steps == 0 ? 1 : 0;
-        o.diff = diff ? 1 : 0;
         o.red_slot = red_slot;
         o.snap_store = 1;
+        // residual: density change in the adsorption pass, |u| sums in the coupling phase
+        const bool vel_res = ctx->coupled && ctx->coupled_b;
+        dev::StepOpt o_psi = o, o_step = o;
+        o_psi.diff = (diff && !vel_res) ? 1 : 0;
+        o_step.diff = (diff && vel_res) ? 1 : 0;
         dim3 grid((unsigned)ll.tile_list.size()), block(256);
         if (!ll.tile_list.empty())
         {
-            if (o.parity == 0) dev::k_ads_psi<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_ads_psi<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            if (o.parity == 0) dev::k_ads_psi<0><<<grid, block, 0, ctx->stream>>>(V, C, o_psi);
+            else dev::k_ads_psi<1><<<grid, block, 0, ctx->stream>>>(V, C, o_psi);
             launch_check(ctx);
-            if (o.parity == 0) dev::k_ads_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o);
-            else dev::k_ads_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o);
+            if (o.parity == 0) dev::k_ads_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o_step);
+            else dev::k_ads_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o_step);
             launch_check(ctx);
         }
         ctx->lv[0].steps++;
         ctx->coarse_done++;
+        if (ctx->coupled && !ctx->coupled_b) ctx->coupled_a++;
         return;
     }
     dev::PhaseArgs a{diff ? 1 : 0, store_u ? 1 : 0, red_slot};
@@ -493,6 +516,8 @@ void checkpoint_save(mgpu_ctx *ctx)
     k.steps.clear();
     for (auto &l : ctx->lv) k.steps.push_back(l.steps);
     k.coarse_done = ctx->coarse_done;
+    k.coupled_a = ctx->coupled_a;
+    k.coupled_b = ctx->coupled_b;
     k.valid = true;
 }
 
@@ -511,6 +536,8 @@ void checkpoint_restore(mgpu_ctx *ctx)
     if (ctx->ibuf.n) CK(cudaMemcpyAsync(ctx->ibuf.p, k.ibuf.p, ctx->ibuf.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     if (ctx->side.n) CK(cudaMemcpyAsync(ctx->side.p, k.side.p, ctx->side.n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->coarse_done = k.coarse_done;
+    ctx->coupled_a = k.coupled_a;
+    ctx->coupled_b = k.coupled_b;
 }
 
 // Steps [k0+1 .. k0+n] with the residual of every step in slots (step index
@@ -546,9 +573,12 @@ void run_batch_with_residuals(mgpu_ctx *ctx, int n)
 // density change, 1e-5 when below 1e-15 (include/coreLB.hpp:1269-1283)
 double residual_of(const mgpu_ctx *ctx, const double *v)
 {
-    if (ctx->adsorption) return v[0] < 1.0e-15 ? 1.0e-5 : v[0];
+    if (ctx->adsorption && !(ctx->coupled && ctx->coupled_b)) return v[0] < 1.0e-15 ? 1.0e-5 : v[0];
     return v[0] / v[1];
 }
+
+// the coupled run leaves its adsorption phase (include/mantiisApp.hpp:378-391)
+void enter_coupling(mgpu_ctx *ctx) { ctx->coupled_b = true; }
 
 std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int only_level)
 {
@@ -842,9 +872,7 @@ void autotune_plain_path(mgpu_ctx *ctx)
 
 void check_supported(mgpu_ctx *ctx)
 {
-    if (ctx->prm.simulation == MGPU_SIM_COUPLED)
-        throw std::runtime_error("the coupled simulation is not available in this build");
-    if (ctx->prm.simulation == MGPU_SIM_ADSORPTION && ctx->grid.max_level > 1)
+    if (ctx->prm.simulation != MGPU_SIM_TRANSPORT && ctx->grid.max_level > 1)
         throw std::runtime_error("the adsorption step is single-block (include/mantiisApp.hpp:248-265 steps level 1 only)");
 }
 } // namespace
@@ -902,7 +930,8 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     go.edge_fine = p->edge_fine != 0;
     ctx->grid = build_grid(img, go);
     if (ctx->grid.max_level > dev::kMaxLevels) throw std::runtime_error("too many refinement levels");
-    ctx->adsorption = p->simulation == MGPU_SIM_ADSORPTION;
+    ctx->adsorption = p->simulation != MGPU_SIM_TRANSPORT;
+    ctx->coupled = p->simulation == MGPU_SIM_COUPLED;
     check_supported(ctx.get());
 
     double rho_init = p->rho_init > 0 ? p->rho_init : ctx->units.rhoin;
@@ -920,6 +949,19 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         lp.collision = COLL_MRT;
     }
     ctx->lay = build_layout(ctx->grid, lp);
+    ImageLayout lay_b; // coupling phase: SRBB wall coefficients and constants
+    if (ctx->coupled)
+    {
+        LayoutParams lpb = lp;
+        lpb.wall = WALL_SRBB;
+        lpb.collision = COLL_RMRT;
+        lay_b = build_layout(ctx->grid, lpb);
+        if (lay_b.specials.size() != ctx->lay.specials.size())
+            throw std::logic_error("coupled run: special records differ between the two wall modes");
+        for (size_t i = 0; i < lay_b.specials.size(); i++)
+            if (lay_b.specials[i].xy != ctx->lay.specials[i].xy)
+                throw std::logic_error("coupled run: special records are ordered differently");
+    }
 
     CK(cudaGetDevice(&ctx->device));
     CK(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device));
@@ -966,6 +1008,12 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     }
     ctx->specials.upload(ctx->lay.specials, acct, s);
     ctx->ktab.upload(ctx->lay.ktab, acct, s);
+    if (ctx->coupled)
+    {
+        ctx->specials_b.upload(lay_b.specials, acct, s);
+        ctx->ktab_b.upload(lay_b.ktab, acct, s);
+        CK(cudaStreamSynchronize(s)); // lay_b's host vectors go out of scope
+    }
     ctx->side.alloc((size_t)ctx->lay.n_quirk * 2, acct);
     ctx->side.zero(s);
     ctx->ibuf.alloc((size_t)ctx->lay.n_buffers * 9, acct);
@@ -1090,6 +1138,10 @@ int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
         while (done < n_steps && !broke)
         {
             int batch = std::min(batch_max, n_steps - done);
+            // a coupled run's adsorption phase ends after 100 steps or on the
+            // residual test; batches do not cross that point
+            const bool phase_a = ctx->coupled && !ctx->coupled_b;
+            if (phase_a) batch = std::min(batch, 100 - ctx->coupled_a);
             checkpoint_save(ctx);
             int64_t k0 = ctx->coarse_done;
             run_batch_with_residuals(ctx, batch);
@@ -1117,12 +1169,14 @@ int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
                 }
                 done += stop + 1;
                 ctx->ref_t += stop; // the breaking step is not counted (include/mantiisApp.hpp:302-350)
-                broke = true;
+                if (phase_a) enter_coupling(ctx); // the break ends the adsorption phase only
+                else broke = true;
             }
             else
             {
                 done += batch;
                 ctx->ref_t += batch;
+                if (phase_a && ctx->coupled_a >= 100) enter_coupling(ctx);
             }
         }
         CK(cudaStreamSynchronize(ctx->stream));
@@ -1149,6 +1203,11 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
         for (int i = 0; i < n_steps; i++)
         {
             int64_t k = ctx->coarse_done + 1;
+            if (ctx->coupled && !ctx->coupled_b && ctx->coupled_a >= 100)
+            {
+                flush(); // residuals of the adsorption phase read as such
+                enter_coupling(ctx);
+            }
             if (ctx->adsorption)
             {
                 bool diff = (k % K == 0);
@@ -1175,6 +1234,7 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
 
 int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
 {
+    if (ctx && ctx->coupled) return mgpu_advance(ctx, n_steps); // its phase switch is host-side
     return guarded(ctx, [&]() {
         if (!ctx || n_steps < 0) throw std::invalid_argument("bad argument");
         int left = n_steps;

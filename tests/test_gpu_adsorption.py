@@ -69,3 +69,27 @@ def test_exponential_pseudopotential_vs_oracle():
     e_ux = np.abs(got["ux"] - ref["ux"]).max() / max(np.abs(ref["ux"]).max(), 1e-30)
     record("adsorption_exponential_128", rho=e_rho, ux=e_ux)
     assert e_rho < 1e-6 and e_ux < 1e-3
+
+
+def test_coupled_run_matches_reference_code(fixture64):
+    # the reference's own coupled run (tests/golden/refstate_coupled64.npz):
+    # 100 adsorption steps without body force, then regularized MRT + Shan-Chen
+    # force + SRBB coupling steps whose velocity residual stays 1
+    from mantiis_gb300 import SIM_COUPLED
+
+    st = load("refstate_coupled64.npz")
+    p = default_params(dx=12e-9, simulation=SIM_COUPLED)
+    s = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], p)
+    done = 0
+    for step in (100, 101, 130):
+        assert s.run(step - done) == step - done
+        done = step
+        c = s.cells(with_f=True)
+        e_f = np.abs(c["f"] - st[f"f_{step}"]).max() / 0.2355
+        umax = np.abs(st[f"ux_{step}"]).max()
+        e_ux = np.abs(c["ux"] - st[f"ux_{step}"]).max() / umax if step > 100 else 0.0
+        e_rho = np.abs(c["rho"] - st[f"rho_{step}"]).max() / np.abs(st[f"rho_{step}"]).max() if step > 100 else 0.0
+        record(f"coupled_64_{step}", f=e_f, ux=e_ux, rho=e_rho)
+        assert e_f < 1e-5 and e_ux < 1e-3 and e_rho < 1e-4
+    r = s.residuals()
+    assert len(r) == 130 and np.allclose(r[100:], 1.0)
