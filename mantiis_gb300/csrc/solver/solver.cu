@@ -177,6 +177,7 @@ struct mgpu_ctx
     // coupled run (include/mantiisApp.hpp:376-392): up to 100 adsorption steps
     // without body force, then coupling steps (regularized MRT, SRBB walls)
     bool coupled = false, coupled_b = false;
+    bool last_step_b = false;            // the last executed step was a coupling step
     int coupled_a = 0;                   // adsorption-phase steps done
     DevBuf<SpecialRec> specials_b;       // records with SRBB wall coefficients / constants
     DevBuf<float> ktab_b;
@@ -202,7 +203,7 @@ struct mgpu_ctx
         std::vector<int64_t> steps;
         int64_t coarse_done = 0;
         int coupled_a = 0;
-        bool coupled_b = false;
+        bool coupled_b = false, last_step_b = false;
         bool valid = false;
     } ckpt;
 
@@ -224,10 +225,12 @@ struct mgpu_ctx
         C.inlet_outlet = 1;
         C.fbody = (float)prm.fbody;
         if (coupled && !coupled_b) C.fbody = 0.0f; // the adsorption phase runs without body force
-        if (coupled && coupled_b)
+        // the collision of the next step follows the phase; the boundary rules
+        // applied when populations are read belong to the step that streamed them
+        if (coupled && coupled_b) C.collision = COLL_RMRT;
+        if (coupled && last_step_b)
         {
             C.wall = WALL_SRBB;
-            C.collision = COLL_RMRT;
             C.inlet_outlet = 0;
             C.specials = specials_b.p;
             C.ktab = ktab_b.p;
@@ -452,6 +455,7 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         ctx->lv[0].steps++;
         ctx->coarse_done++;
         if (ctx->coupled && !ctx->coupled_b) ctx->coupled_a++;
+        if (ctx->coupled) ctx->last_step_b = ctx->coupled_b;
         return;
     }
     dev::PhaseArgs a{diff ? 1 : 0, store_u ? 1 : 0, red_slot};
@@ -518,6 +522,7 @@ void checkpoint_save(mgpu_ctx *ctx)
     k.coarse_done = ctx->coarse_done;
     k.coupled_a = ctx->coupled_a;
     k.coupled_b = ctx->coupled_b;
+    k.last_step_b = ctx->last_step_b;
     k.valid = true;
 }
 
@@ -538,6 +543,7 @@ void checkpoint_restore(mgpu_ctx *ctx)
     ctx->coarse_done = k.coarse_done;
     ctx->coupled_a = k.coupled_a;
     ctx->coupled_b = k.coupled_b;
+    ctx->last_step_b = k.last_step_b;
 }
 
 // Steps [k0+1 .. k0+n] with the residual of every step in slots (step index
