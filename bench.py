@@ -17,6 +17,10 @@ A bench step is one coarse time step of every image of the batch.
             on the host cores, on a bounded sample of the same workload
 
 --impl reference times that CPU implementation alone, as the reference arm.
+--properties N times the pore-property pipeline (skeleton, distance transforms,
+local pore size, Kn) on one seeded N x N disk image instead: the GPU kernels
+through mgpu_pore_properties_gpu (host buffers in and out) against the host
+code of mgpu_pore_properties, and checks that both agree bit for bit.
 Multi-GPU (torchrun): every rank runs its own batch (weak scaling, no
 collective on the data path).
 """
@@ -155,6 +159,32 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_properties(args):
+    from mantiis_gb300 import generate_disks, pore_properties, pore_properties_gpu
+
+    n = args.properties
+    pore = generate_disks(n, max(2, n // 64), max(4, n // 16), 0.6, 5, open_x_edges=True)
+    for _ in range(args.warmup):
+        pore_properties_gpu(pore[: min(n, 256), : min(n, 256)].copy(), 1e-9, 5e-9)
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        lp, kn, iters = pore_properties_gpu(pore, 1e-9, 5e-9, return_iterations=True)
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    lp_h, kn_h = pore_properties(pore, 1e-9, 5e-9)
+    host_s = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "pore_properties_ms", "value": round(1e3 * float(np.median(times)), 3), "unit": "ms",
+        "higher_is_better": False, "steps": len(times), "warmup": args.warmup,
+        "config": {"workload": f"one {n}x{n} seeded disk image (r U[{max(2, n // 64)},{max(4, n // 16)}], "
+                               "porosity 0.6, void x edges)", "thinning_iterations": int(iters)},
+        "host_ms": round(1e3 * host_s, 1), "host_cores": 1,
+        "bit_equal": bool(np.array_equal(lp, lp_h) and np.array_equal(kn, kn_h)),
+        "gpu_launches": 2 * 16 * int(-(-iters // 16)) + 9,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -167,6 +197,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--properties", type=int, default=0, metavar="N")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -174,6 +205,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.properties:
+        run_properties(args)
         return
 
     import torch

@@ -249,6 +249,17 @@ int mgpu_units(double dx, double T, double P, double out[6]);
  * (Shape::calculateProperties, include/shape.hpp:127-251). */
 int mgpu_pore_properties(const int32_t *pore, int n, double dx, double mfp, double *locpore, double *kn);
 
+/* The same fields computed on the current GPU (host pointers in and out, one
+ * synchronous call on `stream`, a cudaStream_t, NULL = legacy default stream):
+ * the Zhang-Suen skeleton of the padded image (utils::thinning,
+ * include/utils.hpp:438-536) as bit-packed bitwise kernels, the two exact
+ * distance transforms (include/shape.hpp:183-212) and the nearest-skeleton
+ * search (utils::distanceToNearestWallIndex, include/utils.hpp:116-135).
+ * Results equal mgpu_pore_properties bit for bit.  4 <= n <= 16384;
+ * `iterations` (may be NULL) receives the number of thinning iterations. */
+int mgpu_pore_properties_gpu(const int32_t *pore, int n, double dx, double mfp, double *locpore, double *kn,
+                             int64_t *iterations, void *stream);
+
 /* Seeded disk packing (synthetic pore images): disks of radius U[rmin, rmax]
  * at uniform centres until the porosity is <= porosity; rows 0 and n-1 solid. */
 int mgpu_generate_disks(int n, double rmin, double rmax, double porosity, uint64_t seed, int32_t *pore_out);

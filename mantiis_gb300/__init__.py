@@ -15,6 +15,7 @@ from .native import (  # noqa: F401
     generate_disks,
     lib,
     pore_properties,
+    pore_properties_gpu,
     units,
 )
 
@@ -26,6 +27,7 @@ __all__ = [
     "default_params",
     "generate_disks",
     "pore_properties",
+    "pore_properties_gpu",
     "units",
     "lib",
     "SIM_TRANSPORT",

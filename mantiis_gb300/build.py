@@ -31,7 +31,7 @@ HOST_SOURCES = [
     "host/capi_host.cpp",
     "solver/layout.cpp",
 ]
-CUDA_SOURCES = ["solver/solver.cu"]
+CUDA_SOURCES = ["solver/solver.cu", "geometry/pore_props.cu"]
 APP_SOURCES = ["app/mantiis_main.cpp"]
 
 

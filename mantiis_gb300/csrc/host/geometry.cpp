@@ -11,6 +11,7 @@
 #include <stdexcept>
 
 #include "../boundary_tables.h"
+#include "medial_search.hpp"
 
 namespace mantiis
 {
@@ -245,19 +246,7 @@ void local_pore_properties(const std::vector<int> &domain, int n, double dx, dou
             size_t k = (size_t)i * n + j;
             if (domain[k] != 1) continue;
             double D = (double)dskel[k];
-            int64_t hit = -1;
-            for (int64_t r = (int64_t)(i - D - 2); r < i + D + 2 && hit < 0; r++)
-                for (int64_t c = (int64_t)(j - D - 2); c < j + D + 2; c++)
-                {
-                    if (r < 0 || r >= n || c < 0 || c >= n) continue;
-                    double di = (double)(i - r), dj = (double)(j - c);
-                    double dist = std::sqrt(di * di + dj * dj);
-                    if (std::fabs(dist - D) < 1.0e-4 && skel[(size_t)r * n + c])
-                    {
-                        hit = r * n + c;
-                        break;
-                    }
-                }
+            int64_t hit = nearest_skeleton_at(skel.data(), n, i, j, D);
             // a void pixel always has a skeleton pixel at its skeleton distance;
             // fall back to its own wall distance should that ever fail
             double mid = hit >= 0 ? (double)dwall[hit] * (double)skel[hit] : (double)dwall[k];

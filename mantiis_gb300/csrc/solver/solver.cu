@@ -18,6 +18,7 @@
 
 #include "../../../include/mantiis_gpu.h"
 #include "../boundary_tables.h"
+#include "../geometry/pore_props.hpp"
 #include "../host/geometry.hpp"
 #include "../host/grid.hpp"
 #include "../host/units.hpp"
@@ -1503,6 +1504,24 @@ double *noalloc_stage(int device)
 } // namespace
 
 extern "C" {
+
+int mgpu_pore_properties_gpu(const int32_t *pore, int n, double dx, double mfp, double *locpore, double *kn,
+                             int64_t *iterations, void *stream)
+{
+    try
+    {
+        gpu_pore_properties(pore, n, dx, mfp, locpore, kn, iterations, static_cast<cudaStream_t>(stream));
+        return MGPU_OK;
+    }
+    catch (const std::invalid_argument &e)
+    {
+        return fail(nullptr, MGPU_E_ARG, e.what());
+    }
+    catch (const std::exception &e)
+    {
+        return fail(nullptr, is_geometry_cuda_error(e) ? MGPU_E_CUDA : MGPU_E_ARG, e.what());
+    }
+}
 
 int mgpu_set_equilibrium_noalloc(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy)
 {

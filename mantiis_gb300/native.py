@@ -118,6 +118,8 @@ SIGNATURES = {
     "mgpu_host_error": (C.c_char_p, []),
     "mgpu_units": (C.c_int, [C.c_double, C.c_double, C.c_double, F64P]),
     "mgpu_pore_properties": (C.c_int, [I32P, C.c_int, C.c_double, C.c_double, F64P, F64P]),
+    "mgpu_pore_properties_gpu": (C.c_int, [I32P, C.c_int, C.c_double, C.c_double, F64P, F64P,
+                                           C.POINTER(C.c_int64), C.c_void_p]),
     "mgpu_generate_disks": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, I32P]),
     "mgpu_generate_disks_ex": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int, I32P]),
 }
@@ -171,6 +173,23 @@ def pore_properties(pore, dx, mfp):
     kn = np.zeros((n, n))
     _host_check(lib().mgpu_pore_properties(pore.reshape(-1), n, dx, mfp, lp.reshape(-1), kn.reshape(-1)))
     return lp, kn
+
+
+def pore_properties_gpu(pore, dx, mfp, stream=None, return_iterations=False):
+    """pore_properties computed by the GPU kernels on the current device (same
+    results bit for bit); optionally also the number of thinning iterations."""
+    pore = np.ascontiguousarray(pore, dtype=np.int32)
+    n = pore.shape[0]
+    if pore.shape != (n, n):
+        raise ValueError("pore image must be square")
+    lp = np.zeros((n, n))
+    kn = np.zeros((n, n))
+    it = C.c_int64(0)
+    rc = lib().mgpu_pore_properties_gpu(pore.reshape(-1), n, dx, mfp, lp.reshape(-1), kn.reshape(-1),
+                                        C.byref(it), stream)
+    if rc != 0:
+        raise MantiisError(rc, lib().mgpu_global_error().decode())
+    return (lp, kn, it.value) if return_iterations else (lp, kn)
 
 
 def generate_disks(n, rmin, rmax, porosity, seed, periodic_x=False, open_x_edges=False):

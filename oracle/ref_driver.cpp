@@ -14,6 +14,10 @@
  *              [--mode transport|adsorption|coupled] [--dx v] [--fbody v]
  *              [--T v] [--P v] [--collision 0|1|2] [--wall 0|1|2] [--tol v]
  *              [--dump dir] [--dump-steps a,b,c] [--no-break] [--quiet]
+ *   --mode properties --mfp v --dx v --dump dir: only Shape::calculateProperties
+ *              (include/shape.hpp:127-251) on pore.dat; writes dir/properties.bin
+ *              (LocPore then Kn, row-major [row][column], as length-prefixed
+ *              float64 vectors).
  */
 #include <omp.h>
 #include <chrono>
@@ -123,6 +127,7 @@ int main(int argc, char *argv[])
     std::string mode = "transport", dumpdir;
     std::set<int> dump_steps;
     bool nobreak = false, quiet = false;
+    double props_mfp = 0.0;
     settings.dx = 1.0e-9;
     settings.Fbody = 1.0e-8;
     for (int a = 6; a < argc; a++)
@@ -140,6 +145,7 @@ int main(int argc, char *argv[])
         else if (k == "--collision") settings.collision_method = std::stoi(next());
         else if (k == "--wall") settings.wall_boundary = std::stoi(next());
         else if (k == "--tol") settings.threshold = std::stod(next());
+        else if (k == "--mfp") props_mfp = std::stod(next());
         else if (k == "--dump") dumpdir = next();
         else if (k == "--dump-steps")
         {
@@ -171,6 +177,21 @@ int main(int argc, char *argv[])
     // ---- MantiisApp::init (include/mantiisApp.hpp:158-237)
     Shape shape(Nx, Ny, _GLOBAL_::Cl);
     shape.loadExistingModel(folder);
+    if (mode == "properties")
+    {
+        shape.calculateProperties(settings.dx, props_mfp);
+        std::ofstream o(dumpdir + "/properties.bin", std::ios::binary);
+        std::vector<double> lp, kn;
+        for (int i = 0; i < Ny; i++)
+            for (int j = 0; j < Nx; j++)
+            {
+                lp.push_back(shape.LocPore[i][j]);
+                kn.push_back(shape.Kn[i][j]);
+            }
+        putv(o, lp);
+        putv(o, kn);
+        return 0;
+    }
     lattice latt;
     Grid2D grid(shape, latt, is_multiblock);
     auto t_setup0 = std::chrono::steady_clock::now();

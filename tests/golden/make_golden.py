@@ -10,8 +10,11 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
   refstate_<case>.npz per-cell state of the reference's own solver after some
                     steps for multi-block cases where the reference's
                     interpolation stays inside its arrays
+  refstate_coupled64.npz  the reference's coupled run on the 64x64 test image
+  refprops.npz      local pore size and Kn from the reference's own
+                    Shape::calculateProperties on four pore images
 
-Usage: python tests/golden/make_golden.py [REF_DIR]
+Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|coupled]
 """
 import os
 import struct
@@ -24,7 +27,11 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+_ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+_ONLY = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+if _ONLY:
+    _ARGS.remove(_ONLY)
+REF = Path(_ARGS[0] if _ARGS else "/root/reference")
 DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
 HOME = ROOT / "oracle" / "_ref" / "home"
 
@@ -155,6 +162,7 @@ def main():
             np.savez_compressed(HERE / f"refstate_{name}.npz",
                                 **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
     coupled_fixture(fx)
+    properties_fixture(fx)
     print("fixtures written to", HERE)
 
 
@@ -170,5 +178,56 @@ def coupled_fixture(fx):
                             **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
 
 
+def run_ref_properties(pore, dx, mfp):
+    """Shape::calculateProperties (include/shape.hpp:127-251) of the reference on
+    one pore image: (LocPore, Kn), row-major [row][column]."""
+    n = pore.shape[0]
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "img"
+        zero = np.zeros((n, n))
+        write_col_major(f, pore, zero, zero)
+        cmd = [str(DRIVER), "1", "False", str(n), str(f) + "/", "0", "--mode", "properties", "--dx", repr(dx),
+               "--mfp", repr(mfp), "--quiet", "--dump", tmp]
+        subprocess.run(cmd, check=True, env=dict(os.environ, HOME=str(HOME)), stdout=subprocess.DEVNULL)
+        raw = (Path(tmp) / "properties.bin").read_bytes()
+    count = int(np.frombuffer(raw[:8], np.int64)[0])
+    lp = np.frombuffer(raw[8:8 + 8 * count], np.float64)
+    kn = np.frombuffer(raw[16 + 8 * count:16 + 16 * count], np.float64)
+    return lp.reshape(n, n).copy(), kn.reshape(n, n).copy()
+
+
+def disk_image(n, rmin, rmax, porosity, seed, open_x_edges=False):
+    """Seeded disk packing of the package's own generator (host code, no GPU)."""
+    sys.path.insert(0, str(ROOT))
+    from mantiis_gb300 import generate_disks
+    return generate_disks(n, rmin, rmax, porosity, seed, open_x_edges=open_x_edges).astype(np.int32)
+
+
+def properties_fixture(fx):
+    """Local pore size and Kn of the reference on four images: the 64x64 test
+    image, disk packings at 128 and 256 (the second with void x edges), and a
+    256 image of a few large disks whose top and bottom rows are partly void."""
+    images = {
+        "fx64": fx["pore"].astype(np.int32),
+        "disks128": disk_image(128, 4, 16, 0.6, 1),
+        "disks256": disk_image(256, 8, 32, 0.6, 2, open_x_edges=True),
+    }
+    big = disk_image(256, 24, 60, 0.8, 3)
+    big[0, 100:180] = 1
+    big[255, 40:90] = 1
+    images["bigpores256"] = big
+    out = {}
+    for name, pore in images.items():
+        lp, kn = run_ref_properties(pore, 1e-9, 5e-9)
+        out[f"{name}_pore"] = pore.astype(np.uint8)
+        out[f"{name}_locpore"] = lp
+        out[f"{name}_kn"] = kn
+    np.savez_compressed(HERE / "refprops.npz", dx=1e-9, mfp=5e-9, **out)
+
+
 if __name__ == "__main__":
-    main()
+    if _ONLY:
+        fx = dict(np.load(HERE / "fixture64.npz"))
+        {"properties": properties_fixture, "coupled": coupled_fixture}[_ONLY](fx)
+    else:
+        main()
