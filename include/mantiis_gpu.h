@@ -170,6 +170,28 @@ int mgpu_reconstructed(const mgpu_ctx *ctx, int64_t *out);
  * reference cell order. */
 int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, const double *uy);
 
+/* Restart from saved populations; no counterpart in the reference, which
+ * writes f.txt (include/mantiisApp.hpp:412, LB2D::prepareDistributions) but
+ * never reads it back.  f becomes the state and the step counter is set to t
+ * (lb->t), so that stepping continues as if the run had not stopped: with the
+ * populations of mgpu_download_cells the continued run equals the
+ * uninterrupted one up to the FP64 rounding of the saved f = w rho0 + df (a
+ * deviation df below ~1e-9 may come back one FP32 ulp off).  Layouts:
+ *   MGPU_LAYOUT_CELLS   9 * n_cells, cell order (mgpu_download_cells);
+ *   MGPU_LAYOUT_PIXELS  9 * n * n, f.txt's order (mgpu_download_pixels): every
+ *                       cell takes the populations of its top-left pixel,
+ *                       exact on single-block grids; on multi-block grids the
+ *                       interface buffer cells take the values of the cells
+ *                       that cover the same pixel.
+ * The residual history starts empty.  The first transport residual after a
+ * restart is the uninterrupted run's; the first adsorption (density) residual
+ * compares the restart state with itself, as the first step of a fresh run does
+ * (the reference's 1e-5 floor).  A coupled run resumes in the phase that t
+ * falls in.  Non-finite populations are rejected (MGPU_E_INPUT). */
+#define MGPU_LAYOUT_CELLS 0
+#define MGPU_LAYOUT_PIXELS 1
+int mgpu_set_distributions(mgpu_ctx *ctx, const double *f, int layout, int64_t t);
+
 /* mgpu_set_equilibrium without any allocation; it has no counterpart in the
  * reference.  For callers that must not allocate device or host memory during a
  * run, e.g. a loop that warm-starts contexts while other contexts keep stepping

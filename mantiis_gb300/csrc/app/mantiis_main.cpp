@@ -11,14 +11,30 @@
 //   --preset mantiis|transport_test|adsorption_test   (default mantiis)
 //   --simulation transport|adsorption  --dx m  --fbody f  --T K  --P Pa
 //   --collision 0|1|2  --wall 0|1|2  --tol t  --levels 2|3  --verbose k
+// and, beyond the reference:
+//   --output text|binary|both   text: the reference's files (default); binary:
+//                               ux.bin uy.bin rho.bin f.bin convergence.bin
+//                               (raw little-endian float64, same order as the
+//                               text files) and f_cells.bin (9 per grid cell,
+//                               the exact restart state)
+//   --restart file [--restart-step t]  start from saved populations: f.txt,
+//                               f.bin (pixel layout) or f_cells.bin (cell
+//                               layout, exact on multi-block grids), told
+//                               apart by their length; t = the step the file
+//                               was written at (SimulationDetails.txt's
+//                               "Number timesteps executed"), default 0
+// Text files are formatted by num_threads threads (argv[1]).
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../../include/mantiis_gpu.h"
@@ -34,17 +50,104 @@ struct Settings
     double threshold = 1.0e-10;
     int collision_method = 2, wall_boundary = 2;
     int levels = 2;
+    std::string output = "text";
+    std::string restart;
+    long long restart_step = 0;
 };
 
+void format_one(std::string &buf, double x)
+{
+    char tmp[40];
+    int k = std::snprintf(tmp, sizeof tmp, "%.15g\n", x); // = ostream << setprecision(15) << x
+    buf.append(tmp, (size_t)k);
+}
+void format_one(std::string &buf, int64_t x)
+{
+    char tmp[32];
+    int k = std::snprintf(tmp, sizeof tmp, "%lld\n", (long long)x);
+    buf.append(tmp, (size_t)k);
+}
+
+int g_threads = 1;
+
+// One value per line, 15 significant digits (include/io.hpp:75-92); the text
+// is formatted in g_threads slices in parallel and written in order.
 template <typename T> void write_vec(const std::string &path, const std::vector<T> &v)
 {
-    std::ofstream out(path);
-    if (!out.is_open())
+    std::FILE *out = std::fopen(path.c_str(), "wb");
+    if (!out)
     {
         std::cout << "Tried writing " << path << std::endl;
         throw std::runtime_error("[ERROR]: Unable to open file for writing.");
     }
-    for (const auto &x : v) out << std::setprecision(15) << x << '\n';
+    const size_t slice = 1 << 18;
+    const size_t n_slices = (v.size() + slice - 1) / slice;
+    const int nt = (int)std::max<size_t>(1, std::min<size_t>((size_t)g_threads, n_slices));
+    bool ok = true;
+    for (size_t first = 0; first < n_slices; first += (size_t)nt)
+    {
+        std::vector<std::string> text((size_t)nt);
+        auto work = [&](int w) {
+            size_t sl = first + (size_t)w;
+            if (sl >= n_slices) return;
+            std::string &b = text[(size_t)w];
+            b.reserve(slice * 24);
+            for (size_t k = sl * slice, end = std::min(v.size(), (sl + 1) * slice); k < end; k++) format_one(b, v[k]);
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nt; w++) pool.emplace_back(work, w);
+        work(0);
+        for (auto &th : pool) th.join();
+        for (auto &b : text) ok = ok && std::fwrite(b.data(), 1, b.size(), out) == b.size();
+    }
+    ok = std::fclose(out) == 0 && ok;
+    if (!ok) throw std::runtime_error("[ERROR]: Unable to write file " + path);
+}
+
+void write_bin(const std::string &path, const std::vector<double> &v)
+{
+    std::FILE *out = std::fopen(path.c_str(), "wb");
+    if (!out) throw std::runtime_error("[ERROR]: Unable to open file for writing.");
+    bool ok = std::fwrite(v.data(), sizeof(double), v.size(), out) == v.size();
+    ok = std::fclose(out) == 0 && ok;
+    if (!ok) throw std::runtime_error("[ERROR]: Unable to write file " + path);
+}
+
+// populations of a restart file: raw float64 (.bin) or whitespace-separated text
+std::vector<double> read_restart(const std::string &path)
+{
+    std::FILE *in = std::fopen(path.c_str(), "rb");
+    if (!in)
+    {
+        std::cout << "Tried loading " << path << std::endl;
+        throw std::runtime_error("[ERROR]: File not found.");
+    }
+    std::string raw;
+    char chunk[1 << 16];
+    size_t k;
+    while ((k = std::fread(chunk, 1, sizeof chunk, in)) > 0) raw.append(chunk, k);
+    std::fclose(in);
+    std::vector<double> v;
+    const bool binary = path.size() >= 4 && path.compare(path.size() - 4, 4, ".bin") == 0;
+    if (binary)
+    {
+        if (raw.size() % sizeof(double)) throw std::runtime_error("[ERROR]: " + path + " is not a float64 file.");
+        v.resize(raw.size() / sizeof(double));
+        std::memcpy(v.data(), raw.data(), raw.size());
+        return v;
+    }
+    const char *p = raw.c_str();
+    char *end = nullptr;
+    for (;;)
+    {
+        double x = std::strtod(p, &end);
+        if (end == p) break;
+        v.push_back(x);
+        p = end;
+    }
+    while (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r') p++;
+    if (*p) throw std::runtime_error("[ERROR]: unreadable number in " + path);
+    return v;
 }
 
 void check(int rc, mgpu_ctx *ctx)
@@ -94,6 +197,9 @@ int main(int argc, char *argv[])
         else if (k == "--tol") st.threshold = std::stod(v);
         else if (k == "--levels") st.levels = std::stoi(v);
         else if (k == "--verbose") st.verbose = std::stoi(v);
+        else if (k == "--output") st.output = v;
+        else if (k == "--restart") st.restart = v;
+        else if (k == "--restart-step") st.restart_step = std::stoll(v);
         else
         {
             std::cerr << "unknown option " << k << "\n";
@@ -112,7 +218,10 @@ int main(int argc, char *argv[])
     try
     {
         int num_threads = std::stoi(argv[1]);
-        (void)num_threads; // host preprocessing is single-threaded here; accepted for compatibility
+        g_threads = std::max(1, std::min(num_threads, 256)); // text output formatting
+        if (st.output != "text" && st.output != "binary" && st.output != "both")
+            throw std::runtime_error("unknown output format " + st.output);
+        const bool text_out = st.output != "binary", bin_out = st.output != "text";
         bool is_multiblock = (std::string(argv[2]) == "true");
         int Nx = std::stoi(argv[3]);
         std::string folder = argv[4];
@@ -158,6 +267,19 @@ int main(int argc, char *argv[])
 
         // run loop (include/mantiisApp.hpp:294-352)
         int64_t t = 0;
+        if (!st.restart.empty())
+        {
+            std::vector<double> f0 = read_restart(st.restart);
+            const size_t per_cell = 9 * (size_t)info.n_cells, per_pixel = 9 * (size_t)Nx * Nx;
+            int layout = f0.size() == per_pixel ? MGPU_LAYOUT_PIXELS : MGPU_LAYOUT_CELLS;
+            if (f0.size() != per_pixel && f0.size() != per_cell)
+                throw std::runtime_error("[ERROR]: " + st.restart + " holds " + std::to_string(f0.size()) +
+                                         " values, expected " + std::to_string(per_pixel) + " (pixels) or " +
+                                         std::to_string(per_cell) + " (cells)");
+            check(mgpu_set_distributions(ctx, f0.data(), layout, st.restart_step), ctx);
+            t = st.restart_step;
+            std::cout << "Restarting from " << st.restart << " at timestep " << t << "\n";
+        }
         std::vector<double> hist;
         int done_total = 0;
         bool stopped = false;
@@ -168,16 +290,19 @@ int main(int argc, char *argv[])
             mgpu_residuals(ctx, hist.data(), cnt, &cnt);
         };
         const bool coupled = p.simulation == MGPU_SIM_COUPLED;
-        if (coupled)
+        if (coupled && t < 100)
         {
             // 100 adsorption steps come first (include/mantiisApp.hpp:376-392)
-            iters += 100;
+            iters += (int)(100 - t);
             std::cout << "======================= Adsorption ONLY for initial condition =======================\n";
         }
         while (done_total < iters && !stopped)
         {
-            // first step alone (its fields are dumped as ux_0 / uy_0), then in chunks
-            int chunk = done_total == 0 ? 1 : std::min(iters - done_total, 1000);
+            // chunks of up to 1000 steps that end on every step whose fields are
+            // dumped (ux_<t>, uy_<t>: t = 0, then every dump_macroscopic_every_timestep)
+            const long long every = st.dump_macroscopic_every_timestep;
+            const long long to_dump = (every - t % every) % every;
+            int chunk = (int)std::min<long long>({(long long)(iters - done_total), 1000LL, to_dump + 1});
             size_t h0 = hist.size();
             int done = 0;
             check(mgpu_run(ctx, chunk, &done), ctx);
@@ -209,11 +334,25 @@ int main(int argc, char *argv[])
         size_t nn = (size_t)Nx * Nx;
         std::vector<double> rho(nn), ux(nn), uy(nn), f(nn * 9);
         check(mgpu_download_pixels(ctx, rho.data(), ux.data(), uy.data(), f.data()), ctx);
-        write_vec(folder + "f.txt", f);
-        write_vec(folder + "ux.txt", ux);
-        write_vec(folder + "uy.txt", uy);
-        write_vec(folder + "rho.txt", rho);
-        write_vec(folder + "convergence.txt", hist);
+        if (text_out)
+        {
+            write_vec(folder + "f.txt", f);
+            write_vec(folder + "ux.txt", ux);
+            write_vec(folder + "uy.txt", uy);
+            write_vec(folder + "rho.txt", rho);
+            write_vec(folder + "convergence.txt", hist);
+        }
+        if (bin_out)
+        {
+            std::vector<double> fc(9 * (size_t)info.n_cells);
+            check(mgpu_download_cells(ctx, nullptr, nullptr, nullptr, fc.data()), ctx);
+            write_bin(folder + "f_cells.bin", fc);
+            write_bin(folder + "f.bin", f);
+            write_bin(folder + "ux.bin", ux);
+            write_bin(folder + "uy.bin", uy);
+            write_bin(folder + "rho.bin", rho);
+            write_bin(folder + "convergence.bin", hist);
+        }
         std::ofstream det(folder + "SimulationDetails.txt");
         det << "Domain dimension: " << Nx << " x " << Nx << "\n";
         det << "Tolerance was set to " << st.threshold << "\n";

@@ -836,5 +836,44 @@ __global__ void k_set_equilibrium(AllLevels A, Common C, const int32_t *cell_lev
             for (int q = 0; q < 9; q++) C.ibuf[(size_t)q * C.n_buf + rec.buf] = df[q];
     }
 }
+// Restart: the populations f (FP64, 9 per cell in cell order) become the state
+// in the slots the first step reads directly, as after k_set_equilibrium; the
+// residual side arrays take the moments of f with the FP32 arithmetic of a step.
+__global__ void k_set_distributions(AllLevels A, Common C, const int32_t *cell_level, const int32_t *cell_site,
+                                    int64_t n, const double *f)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int l = cell_level[c] - 1;
+    const LevelView &L = A.lv[l];
+    const int s = cell_site[c];
+    float df[9];
+    for (int q = 0; q < 9; q++)
+    {
+        df[q] = (float)(f[c * 9 + q] - d2q9::w(q) * (double)C.rho0);
+        L.f[(size_t)q * L.plane + s] = df[q];
+    }
+    float drho, rho, ux, uy;
+    macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
+    if (L.unorm) L.unorm[s] = sqrtf(ux * ux + uy * uy);
+    if (L.rho_prev)
+    {
+        float sum = 0.0f;
+        for (int q = 0; q < 9; q++) sum += df[q];
+        L.rho_prev[s] = C.rho0 + sum;
+    }
+    if (L.snap)
+    {
+        L.snap[s] = drho;
+        L.snap[L.plane + s] = ux;
+        L.snap[2 * L.plane + s] = uy;
+    }
+    if (L.omega[s] < 0.0f)
+    {
+        const SpecialRec rec = C.specials[L.spec[s]];
+        if (((rec.m1 >> 17) & 0xFu) & SF_BUFFER)
+            for (int q = 0; q < 9; q++) C.ibuf[(size_t)q * C.n_buf + rec.buf] = df[q];
+    }
+}
 } // namespace dev
 } // namespace mantiis

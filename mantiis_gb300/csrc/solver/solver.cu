@@ -1468,6 +1468,48 @@ int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, con
     });
 }
 
+int mgpu_set_distributions(mgpu_ctx *ctx, const double *f, int layout, int64_t t)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || !f) throw std::invalid_argument("null argument");
+        if (layout != MGPU_LAYOUT_CELLS && layout != MGPU_LAYOUT_PIXELS)
+            throw std::invalid_argument("mgpu_set_distributions: unknown layout " + std::to_string(layout));
+        if (t < 0) throw std::invalid_argument("mgpu_set_distributions: negative time step");
+        const Grid &g = ctx->grid;
+        const int64_t n = g.n_cells;
+        std::vector<double> cells((size_t)n * 9);
+        if (layout == MGPU_LAYOUT_CELLS)
+            std::copy(f, f + n * 9, cells.begin());
+        else
+            for (int64_t c = 0; c < n; c++)
+            {
+                const int64_t px = (int64_t)g.y[c] * g.n + g.x[c];
+                std::copy(f + px * 9, f + px * 9 + 9, cells.begin() + c * 9);
+            }
+        for (double v : cells)
+            if (!std::isfinite(v)) throw std::invalid_argument("mgpu_set_distributions: non-finite population");
+        int64_t tmp = 0;
+        DevBuf<double> df;
+        df.upload(cells, tmp, ctx->stream);
+        for (auto &l : ctx->lv) l.steps = 0;
+        dev::k_set_distributions<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, df.p);
+        launch_check(ctx);
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->ref_t = t;
+        ctx->residuals.clear();
+        ctx->ckpt.valid = false;
+        if (ctx->coupled)
+        {
+            // the first 100 steps of a coupled run are adsorption steps
+            ctx->coupled_a = (int)std::min<int64_t>(t, 100);
+            ctx->coupled_b = t >= 100;
+            ctx->last_step_b = t > 100;
+        }
+        return MGPU_OK;
+    });
+}
+
 } // extern "C"
 
 namespace

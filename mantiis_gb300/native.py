@@ -95,6 +95,7 @@ SIGNATURES = {
     "mgpu_reconstructed": (C.c_int, [P, I64P]),
     "mgpu_cell_positions": (C.c_int, [P, P, P, P]),
     "mgpu_set_equilibrium": (C.c_int, [P, F64P, F64P, F64P]),
+    "mgpu_set_distributions": (C.c_int, [P, F64P, C.c_int, C.c_int64]),
     "mgpu_set_equilibrium_noalloc": (C.c_int, [P, F64P, F64P, F64P]),
     "mgpu_set_stream": (C.c_int, [P, P]),
     "mgpu_launch_count": (C.c_int64, [P]),
@@ -369,6 +370,16 @@ class Solver:
     def set_equilibrium(self, rho, ux, uy):
         a = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in (rho, ux, uy)]
         self._check(lib().mgpu_set_equilibrium(self._h, *a))
+
+    def set_distributions(self, f, layout="cells", t=0):
+        """Restart from populations (mgpu_set_distributions): f of
+        download_cells (layout "cells", 9 per cell) or of f.txt / pixels()
+        (layout "pixels", 9 per pixel); stepping continues from time step t."""
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        want = 9 * (self.n_cells if layout == "cells" else self.n * self.n)
+        if layout not in ("cells", "pixels") or f.size != want:
+            raise ValueError(f"expected {want} populations for layout {layout!r}, got {f.size}")
+        self._check(lib().mgpu_set_distributions(self._h, f, 0 if layout == "cells" else 1, int(t)))
 
     def set_equilibrium_noalloc(self, rho, ux, uy):
         """set_equilibrium staged through the library's static device array
