@@ -271,6 +271,8 @@ def main():
     prof.set_stream(stream.cuda_stream)
     prof.advance(2)
     lvl1 = prof.level_info(1)
+    plain_kernels = {0: "k_phase_plain", 1: "k_phase_plain_tma + k_phase_plain", 2: "k_phase_plain8"}[
+        prof.info["plain_path"]]
     reps = 200
     prof.step_level(1, 10)
     torch.cuda.synchronize()
@@ -328,7 +330,7 @@ def main():
                        "graph": "one CUDA graph of 2 coarse steps for the whole batch (one launch per phase over all images)", "state_finite_after_timed_steps": finite},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "level-1 substep (k_phase_plain_tma + k_phase_plain + k_phase_special)", "units_per_launch": lvl1["active"],
+                         "kernel": f"level-1 substep ({plain_kernels} + k_phase_special)", "units_per_launch": lvl1["active"],
                          "bytes_per_unit": BYTES_PER_LU, "ms_per_launch": k_ms},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,

@@ -56,9 +56,11 @@ typedef struct mgpu_params
     int edge_fine;         /* 1: keep the quadtree at the finest level on the x-periodic edges (the
                               reference's grid, 0, leaves coarse/fine interfaces across that boundary
                               without buffer cells, which makes the multi-block solution diverge) */
-    int plain_path;        /* plain cells of x-interior tiles: 1 = TMA pipeline through shared memory
-                              (default), 0 = direct loads; -1 = pick the faster per image by timing
-                              both at creation (autotune) */
+    int plain_path;        /* plain-cell kernels: 1 = TMA pipeline through shared memory for x-interior
+                              32x8 tiles, 0 = direct loads over 32x8 tiles, 2 = direct loads over 8x4
+                              tiles, one warp each (fits sparse levels better); -1 (default) = pick the
+                              fastest per image by timing all three over a few coarse steps at creation
+                              (the state is put back; results are bit-identical on every path) */
 } mgpu_params;
 
 /* Static description of a built context. */
@@ -76,9 +78,9 @@ typedef struct mgpu_info
     double tau_mean;       /* mean tau_s over non-buffer cells (permeability viscosity) */
     int64_t device_bytes;  /* device memory held by the context */
     int64_t grid_undefined_cases; /* reference-undefined cases given a defined meaning */
-    int plain_path;        /* plain-cell path in use: 1 TMA pipeline, 0 direct loads */
+    int plain_path;        /* plain-cell path in use: 1 TMA pipeline, 0 direct 32x8, 2 direct 8x4 */
     int pad_;
-    double autotune_us[2]; /* plain_path -1: measured microseconds per coarse step, direct / TMA (else 0) */
+    double autotune_us[3]; /* plain_path -1: measured microseconds per coarse step of paths 0, 1, 2 (else 0) */
 } mgpu_info;
 
 void mgpu_default_params(mgpu_params *p);

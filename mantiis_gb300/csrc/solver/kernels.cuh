@@ -203,6 +203,30 @@ __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, 
     }
 }
 
+// Plain cells of one 8x4 tile, one warp per tile (lane = 8 * row + column):
+// the same cell update as plain_tile; on sparse levels these tiles hold a
+// larger share of active cells than 32x8 tiles, so fewer lanes idle and fewer
+// sectors are fetched for inactive sites.
+template <int P>
+__device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C, const StepOpt &o, int t, int diff,
+                                            int store_u, double &r_diff, double &r_norm)
+{
+    const int lane = threadIdx.x & 31;
+    const int tile = __ldg(&L.tiles8[t]); // tx | ty << 16, in 8- and 4-site units
+    const uint32_t mask = __ldg(&L.tile8_mask[t]);
+    if (!((mask >> lane) & 1u)) return;
+    const int tx = tile & 0xFFFF, ty = tile >> 16;
+    const int x = tx * 8 + (lane & 7), y = ty * 4 + (lane >> 3);
+    // tiles off the border reach their neighbours without wrapping
+    const bool interior = tx > 0 && tx + 1 < (L.W + 7) / 8 && ty > 0 && ty + 1 < (L.H + 3) / 4;
+    const int64_t s = site_of(L, x, y);
+    float df[9];
+    load_raw_ro<P>(L, x, y, df, interior);
+    const float om = __ldg(&L.omega[s]);
+    SpecialRec none;
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior);
+}
+
 // One special cell (wall links, missing arrivals, interface buffer, inlet /
 // outlet) from its record.
 template <int P>
@@ -279,6 +303,22 @@ __global__ void __launch_bounds__(256, 5) k_phase_plain(const __grid_constant__ 
     double r_diff = 0.0, r_norm = 0.0;
     if (d.o.parity) plain_tile<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
     else plain_tile<0>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+    if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
+}
+
+// plain cells in 8x4 tiles: 8 tiles (warps) per block
+__global__ void __launch_bounds__(256, 5) k_phase_plain8(const __grid_constant__ PhaseLaunch P)
+{
+    const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
+    const StepDesc &d = P.d[j];
+    const int t = ((int)blockIdx.x - P.start[j]) * 8 + (int)(threadIdx.x >> 5);
+    const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
+    double r_diff = 0.0, r_norm = 0.0;
+    if (t < d.L.ntiles8)
+    {
+        if (d.o.parity) plain_tile8<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+        else plain_tile8<0>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+    }
     if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
 }
 

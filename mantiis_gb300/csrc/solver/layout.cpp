@@ -12,6 +12,17 @@ namespace mantiis
 {
 namespace
 {
+// ordering key of a special record's site (x | y << 16): 8x4 blocks in row-major
+// order, then row-major inside the block
+inline uint64_t special_order_key(int32_t xy)
+{
+    const uint64_t x = (uint64_t)(xy & 0xFFFF), y = (uint64_t)((uint32_t)xy >> 16);
+    return ((y >> 2) << 40) | ((x >> 3) << 20) | ((y & 3) << 8) | (x & 7);
+}
+} // namespace
+
+namespace
+{
 // Node slopes of the three-node cubic spline with parabolically terminated
 // ends (the end intervals are parabolas): closed-form solution of
 //   d0 + d1 = 2 s0,  d0/h0 + 2 (1/h0 + 1/h1) d1 + d2/h1 = 3 (s0/h0 + s1/h1),  d1 + d2 = 2 s1
@@ -262,14 +273,15 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         L.specials.push_back(rec);
         spec_level.push_back(l);
     }
-    // special records grouped by level and sorted by site, so the special-cell
-    // kernel of a level walks a contiguous, spatially ordered range
+    // special records grouped by level and ordered by 8x4 block of sites (row-major
+    // blocks, row-major inside a block), so a warp of the special-cell kernel
+    // covers a compact patch and its neighbour reads share sectors
     {
         std::vector<int64_t> order(L.specials.size());
         for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
         std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
             if (spec_level[a] != spec_level[b]) return spec_level[a] < spec_level[b];
-            return L.specials[a].xy < L.specials[b].xy; // row-major order
+            return special_order_key(L.specials[a].xy) < special_order_key(L.specials[b].xy);
         });
         std::vector<SpecialRec> sorted(order.size());
         for (size_t i = 0; i < order.size(); i++) sorted[i] = L.specials[order[i]];
@@ -324,6 +336,31 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
                 lv.tile_mask.push_back(m);
             }
         }
+    }
+
+    // 8x4 tiles holding a plain cell, row-major (one warp per tile in the
+    // direct 8x4 kernel; sparse levels fill them better than 32x8 tiles)
+    for (auto &lv : L.levels)
+    {
+        const int t8x = (lv.W + 7) / 8, t8y = (lv.H + 3) / 4;
+        for (int ty = 0; ty < t8y; ty++)
+            for (int tx = 0; tx < t8x; tx++)
+            {
+                uint32_t m = 0;
+                for (int r = 0; r < 4; r++)
+                {
+                    const int yy = ty * 4 + r;
+                    if (yy >= lv.H) break;
+                    for (int k = 0; k < 8; k++)
+                    {
+                        const int xx = tx * 8 + k;
+                        if (xx < lv.W && lv.omega[(size_t)yy * lv.pitch + xx] > 0.0f) m |= 1u << (8 * r + k);
+                    }
+                }
+                if (!m) continue;
+                lv.tile8_list.push_back(tx | ty << 16);
+                lv.tile8_mask.push_back(m);
+            }
     }
 
     // interfaces (include/coreLB.hpp:1101-1231)

@@ -76,6 +76,8 @@ struct LevelLayout
     int n_tiles_interior = 0;        // tiles with tx in [1, tiles_x - 2] (no x wrap within one cell)
     std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
     int tiles_x = 0, tiles_y = 0;
+    std::vector<int32_t> tile8_list;  // 8x4 tiles holding a plain cell: tx | ty << 16 (x in 8s, y in 4s)
+    std::vector<uint32_t> tile8_mask; // per such tile, its plain cells (bit = 8 * row + column)
     int64_t n_active = 0, n_active_real = 0;
     int substeps = 1;                // per coarse step, 2^(L-l)
     int64_t spec_begin = 0, spec_count = 0; // this level's special records (sorted by site)

@@ -108,10 +108,11 @@ struct LevelDev
     CUtensorMap tmap;    // the 9 planes as a (x, y, q) tensor for the TMA tile loads
     CUtensorMap om_map;  // the relaxation rates as a (x, y) tensor
     bool has_tmap = false;
+    bool use8 = false;   // plain cells through the 8x4 warp-tile kernel
     DevBuf<float> f, omega, tau2, snap, unorm, psi, rho_prev;
     DevBuf<uint32_t> spec;
-    DevBuf<int32_t> tiles;
-    DevBuf<uint32_t> tile_mask;
+    DevBuf<int32_t> tiles, tiles8;
+    DevBuf<uint32_t> tile_mask, tile8_mask;
     int64_t steps = 0; // substeps done at this level
 };
 
@@ -131,6 +132,7 @@ constexpr int kRing = 8192; // residual accumulator slots (4 doubles each)
 struct PhaseVariant
 {
     std::vector<std::vector<dev::PhaseLaunch>> plain; // per phase: plain cells, tiles with direct loads
+    std::vector<std::vector<dev::PhaseLaunch>> plain8; // per phase: plain cells, 8x4 warp tiles
     std::vector<std::vector<dev::TmaLaunch>> tma;     // per phase: plain cells, x-interior tiles through TMA
     std::vector<std::vector<dev::PhaseLaunch>> spec;  // per phase: special cells
     std::vector<std::vector<dev::WaveLaunch>> waves;        // per wave
@@ -150,6 +152,37 @@ struct PhasePlan
 
 } // namespace
 
+// Streams that run beside a context's (or a batch's) main stream within a
+// phase: the special-cell kernels on one, the x-border plain tiles on the
+// other, so both overlap the x-interior tile kernel.  The three sets of cells
+// own disjoint slots (AA pattern), so no ordering is needed among them.
+struct SideLanes
+{
+    cudaStream_t special = nullptr, border = nullptr;
+    cudaEvent_t fork = nullptr, join_special = nullptr, join_border = nullptr;
+    void create()
+    {
+        CK(cudaStreamCreateWithFlags(&special, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&border, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&join_special, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&join_border, cudaEventDisableTiming));
+    }
+    void destroy()
+    {
+        for (cudaStream_t st : {special, border})
+            if (st)
+            {
+                cudaStreamSynchronize(st);
+                cudaStreamDestroy(st);
+            }
+        for (cudaEvent_t e : {fork, join_special, join_border})
+            if (e) cudaEventDestroy(e);
+        special = border = nullptr;
+        fork = join_special = join_border = nullptr;
+    }
+};
+
 struct mgpu_ctx
 {
     mgpu_params prm{};
@@ -159,8 +192,7 @@ struct mgpu_ctx
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    cudaStream_t side_stream = nullptr; // special-cell kernels, forked from / joined to `stream`
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    SideLanes lanes; // special cells and x-border tiles beside `stream`
     int64_t bytes = 0;
     int64_t launches = 0;
     std::string err;
@@ -189,7 +221,7 @@ struct mgpu_ctx
     std::unique_ptr<PhasePlan> plan; // phase engine tables of this image
     std::vector<std::unique_ptr<PhasePlan>> level_plans; // single-level tables (mgpu_step_level)
     int sm_count = 1;
-    double autotune_us[2] = {0.0, 0.0}; // plain_path -1: direct / TMA microseconds per coarse step
+    double autotune_us[3] = {0.0, 0.0, 0.0}; // plain_path -1: microseconds per coarse step of paths 0, 1, 2
     int64_t coarse_done = 0;     // coarse steps executed since creation
     int64_t ref_t = 0;           // reference lb->t
     std::vector<double> residuals;
@@ -264,6 +296,9 @@ struct mgpu_ctx
         v.tile_mask = d.tile_mask.p;
         v.ntiles = (int)ll.tile_list.size();
         v.tiles_x = ll.tiles_x;
+        v.tiles8 = d.tiles8.p;
+        v.tile8_mask = d.tile8_mask.p;
+        v.ntiles8 = (int)ll.tile8_list.size();
         v.W = ll.W;
         v.H = ll.H;
         v.pitch = ll.pitch;
@@ -417,11 +452,10 @@ void launch_check(mgpu_ctx *ctx)
 std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int only_level);
 std::string state_key(const std::vector<mgpu_ctx *> &ctxs, int ahead);
 PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, int ahead);
-void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::TmaLaunch> &tma,
-                  const std::vector<dev::PhaseLaunch> &spec, const dev::PhaseArgs &a, cudaStream_t main,
-                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int64_t &launches);
-void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, cudaStream_t side,
-                cudaEvent_t fork, cudaEvent_t join, dev::PhaseArgs a, int64_t &launches);
+void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaStream_t main, SideLanes &lanes,
+                  int64_t &launches);
+void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, SideLanes &lanes,
+                dev::PhaseArgs a, int64_t &launches);
 
 // ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
 void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
@@ -460,7 +494,7 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         return;
     }
     dev::PhaseArgs a{diff ? 1 : 0, store_u ? 1 : 0, red_slot};
-    phase_step(*ctx->plan, {ctx}, ctx->stream, ctx->side_stream, ctx->ev_fork, ctx->ev_join, a, ctx->launches);
+    phase_step(*ctx->plan, {ctx}, ctx->stream, ctx->lanes, a, ctx->launches);
 }
 
 // read pass over all reference cells
@@ -525,6 +559,22 @@ void checkpoint_save(mgpu_ctx *ctx)
     k.coupled_b = ctx->coupled_b;
     k.last_step_b = ctx->last_step_b;
     k.valid = true;
+}
+
+// frees the checkpoint buffers (the next save allocates them again)
+void checkpoint_release(mgpu_ctx *ctx)
+{
+    auto &k = ctx->ckpt;
+    int64_t held = 0;
+    for (auto &b : k.f) held += (int64_t)b->n * 4;
+    for (auto &b : k.unorm) held += (int64_t)b->n * 4;
+    held += (int64_t)(k.ibuf.n + k.side.n) * 4;
+    k.f.clear();
+    k.unorm.clear();
+    k.ibuf = DevBuf<float>();
+    k.side = DevBuf<float>();
+    k.valid = false;
+    ctx->bytes -= held;
 }
 
 void checkpoint_restore(mgpu_ctx *ctx)
@@ -674,11 +724,12 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
     };
     PhaseVariant V;
     V.plain.resize(P.nphase);
+    V.plain8.resize(P.nphase);
     V.tma.resize(P.nphase);
     V.spec.resize(P.nphase);
     for (int ph = 0; ph < P.nphase; ph++)
     {
-        std::vector<std::pair<dev::StepDesc, int>> pl, tm, sp;
+        std::vector<std::pair<dev::StepDesc, int>> pl, p8, tm, sp;
         std::vector<const LevelDev *> tm_map;
         for (const int4 &e : P.entries[ph])
         {
@@ -700,8 +751,13 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
             sd.spec_count = (int)ll.spec_count;
             // x-interior tiles through the TMA pipeline (when the image uses it),
             // the others with direct loads
-            const int nt = (int)ll.tile_list.size();
-            const int ni = c->lv[l].has_tmap ? ll.n_tiles_interior : 0;
+            const int nt = c->lv[l].use8 ? 0 : (int)ll.tile_list.size();
+            const int ni = c->lv[l].has_tmap && !c->lv[l].use8 ? ll.n_tiles_interior : 0;
+            if (c->lv[l].use8 && !ll.tile8_list.empty())
+            {
+                sd.tile_base = 0;
+                p8.push_back({sd, (int)((ll.tile8_list.size() + 7) / 8)});
+            }
             if (ni > 0)
             {
                 sd.tile_base = 0;
@@ -717,6 +773,7 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
             if (ll.spec_count) sp.push_back({sd, (int)((ll.spec_count + 127) / 128)});
         }
         V.plain[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(pl);
+        V.plain8[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(p8);
         V.spec[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(sp);
         V.tma[ph] = pack_launches<dev::TmaLaunch, dev::StepDesc, dev::kMaxTmaDescs>(tm);
         for (size_t k = 0; k < V.tma[ph].size(); k++)
@@ -768,15 +825,19 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
 // The launches of one phase: plain cells on `main` (TMA tiles, direct-load
 // tiles), special cells forked onto `side` (their slot sets are disjoint
 // under the AA ownership rule).
-void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<dev::TmaLaunch> &tma,
-                  const std::vector<dev::PhaseLaunch> &spec, const dev::PhaseArgs &a, cudaStream_t main,
-                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int64_t &launches)
+void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaStream_t main, SideLanes &lanes,
+                  int64_t &launches)
 {
-    const bool both = (!plain.empty() || !tma.empty()) && !spec.empty();
-    if (both)
+    const auto &plain = V.plain[ph], &plain8 = V.plain8[ph], &spec = V.spec[ph];
+    const auto &tma = V.tma[ph];
+    // x-border tiles beside the TMA tile kernel, special cells beside the plain kernels
+    const bool border_side = !plain.empty() && !tma.empty();
+    const bool special_side = !spec.empty() && (!plain.empty() || !tma.empty() || !plain8.empty());
+    if (border_side || special_side)
     {
-        CK(cudaEventRecord(fork, main));
-        CK(cudaStreamWaitEvent(side, fork, 0));
+        CK(cudaEventRecord(lanes.fork, main));
+        if (border_side) CK(cudaStreamWaitEvent(lanes.border, lanes.fork, 0));
+        if (special_side) CK(cudaStreamWaitEvent(lanes.special, lanes.fork, 0));
     }
     for (const auto &t0 : tma)
     {
@@ -786,11 +847,19 @@ void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<
         CK(cudaGetLastError());
         launches++;
     }
+    for (const auto &l0 : plain8)
+    {
+        dev::PhaseLaunch l = l0;
+        l.a = a;
+        dev::k_phase_plain8<<<(unsigned)l.start[l.ndesc], 256, 0, main>>>(l);
+        CK(cudaGetLastError());
+        launches++;
+    }
     for (const auto &l0 : plain)
     {
         dev::PhaseLaunch l = l0;
         l.a = a;
-        dev::k_phase_plain<<<(unsigned)l.start[l.ndesc], 256, 0, main>>>(l);
+        dev::k_phase_plain<<<(unsigned)l.start[l.ndesc], 256, 0, border_side ? lanes.border : main>>>(l);
         CK(cudaGetLastError());
         launches++;
     }
@@ -798,21 +867,26 @@ void launch_phase(const std::vector<dev::PhaseLaunch> &plain, const std::vector<
     {
         dev::PhaseLaunch l = l0;
         l.a = a;
-        dev::k_phase_special<<<(unsigned)l.start[l.ndesc], 128, 0, both ? side : main>>>(l);
+        dev::k_phase_special<<<(unsigned)l.start[l.ndesc], 128, 0, special_side ? lanes.special : main>>>(l);
         CK(cudaGetLastError());
         launches++;
     }
-    if (both)
+    if (border_side)
     {
-        CK(cudaEventRecord(join, side));
-        CK(cudaStreamWaitEvent(main, join, 0));
+        CK(cudaEventRecord(lanes.join_border, lanes.border));
+        CK(cudaStreamWaitEvent(main, lanes.join_border, 0));
+    }
+    if (special_side)
+    {
+        CK(cudaEventRecord(lanes.join_special, lanes.special));
+        CK(cudaStreamWaitEvent(main, lanes.join_special, 0));
     }
 }
 
 // One coarse step of every image of the group: the phases, then the
 // interface waves.
-void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, cudaStream_t side,
-                cudaEvent_t fork, cudaEvent_t join, dev::PhaseArgs a, int64_t &launches)
+void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, SideLanes &lanes,
+                dev::PhaseArgs a, int64_t &launches)
 {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(main, &cs));
@@ -821,7 +895,7 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     PhaseVariant &V = plan_variant(P, ctxs, 0);
     const dev::PhaseArgs none{0, 0, 0};
     for (int ph = 0; ph < P.nphase; ph++)
-        launch_phase(V.plain[ph], V.tma[ph], V.spec[ph], ph == 0 ? a : none, main, side, fork, join, launches);
+        launch_phase(V, ph, ph == 0 ? a : none, main, lanes, launches);
     for (int w = 0; w < P.nwave; w++)
         for (const auto &l : V.waves[w])
         {
@@ -836,13 +910,12 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     }
 }
 
-// plain_path -1: times both plain-cell paths over a few coarse steps from the
-// initial state, puts the state back and keeps the faster path.
+// plain_path -1: times the three plain-cell paths (0 direct 32x8 tiles, 1 TMA
+// pipeline for x-interior 32x8 tiles, 2 direct 8x4 warp tiles) over a few
+// coarse steps from the initial state, puts the state back after each and
+// keeps the fastest.
 void autotune_plain_path(mgpu_ctx *ctx)
 {
-    bool any = false;
-    for (auto &l : ctx->lv) any |= l.has_tmap;
-    if (!any) return;
     std::vector<bool> had;
     for (auto &l : ctx->lv) had.push_back(l.has_tmap);
     cudaEvent_t e0, e1;
@@ -850,11 +923,18 @@ void autotune_plain_path(mgpu_ctx *ctx)
     CK(cudaEventCreate(&e1));
     checkpoint_save(ctx);
     const int64_t launches0 = ctx->launches;
-    double us[2] = {0.0, 0.0};
-    for (int path = 0; path < 2; path++)
-    {
-        for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].has_tmap = path == 1 && had[l];
+    double us[3] = {0.0, 0.0, 0.0};
+    auto select = [&](int path) {
+        for (size_t l = 0; l < ctx->lv.size(); l++)
+        {
+            ctx->lv[l].has_tmap = path == 1 && had[l];
+            ctx->lv[l].use8 = path == 2;
+        }
         ctx->plan = build_plan({ctx}, -1);
+    };
+    for (int path = 0; path < 3; path++)
+    {
+        select(path);
         for (int i = 0; i < 2; i++) coarse_step(ctx, false, false, 0);
         const int n = 6;
         CK(cudaEventRecord(e0, ctx->stream));
@@ -869,12 +949,13 @@ void autotune_plain_path(mgpu_ctx *ctx)
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaEventDestroy(e0));
     CK(cudaEventDestroy(e1));
-    const bool tma = us[1] < us[0];
-    for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].has_tmap = tma && had[l];
-    ctx->plan = build_plan({ctx}, -1);
-    ctx->autotune_us[0] = us[0];
-    ctx->autotune_us[1] = us[1];
+    int best = 0;
+    for (int path = 1; path < 3; path++)
+        if (us[path] < us[best]) best = path;
+    select(best);
+    for (int path = 0; path < 3; path++) ctx->autotune_us[path] = us[path];
     ctx->launches = launches0;
+    checkpoint_release(ctx);
 }
 
 void check_supported(mgpu_ctx *ctx)
@@ -909,7 +990,7 @@ void mgpu_default_params(mgpu_params *p)
     p->seed = 0;
     p->check_every = 1;
     p->edge_fine = 0;
-    p->plain_path = 1;
+    p->plain_path = -1;
 }
 
 static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **out)
@@ -974,9 +1055,7 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     CK(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device));
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
-    CK(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    ctx->lanes.create();
     upload_constants();
     cudaStream_t s = ctx->stream;
     int64_t &acct = ctx->bytes;
@@ -997,6 +1076,9 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
         d.spec.upload(ll.spec, acct, s);
         d.tiles.upload(ll.tile_list, acct, s);
         d.tile_mask.upload(ll.tile_mask, acct, s);
+        d.tiles8.upload(ll.tile8_list, acct, s);
+        d.tile8_mask.upload(ll.tile8_mask, acct, s);
+        d.use8 = p->plain_path == 2 && !ctx->adsorption;
         d.unorm.alloc((size_t)ll.plane, acct);
         d.unorm.zero(s);
         if (ll.snapshot_all || ctx->adsorption)
@@ -1097,10 +1179,7 @@ int mgpu_destroy(mgpu_ctx *ctx)
     if (!ctx) return MGPU_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-    if (ctx->side_stream) cudaStreamSynchronize(ctx->side_stream);
-    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
-    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    ctx->lanes.destroy();
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MGPU_OK;
@@ -1128,9 +1207,10 @@ int mgpu_get_info(const mgpu_ctx *ctx, mgpu_info *info)
         d.buffer_wall_links + d.fine_parent_missing_nbr + d.coarse_missing_child + d.fine_group_unmatched + d.pore_search_failed;
     bool tma = false;
     for (auto &l : ctx->lv) tma |= l.has_tmap;
-    info->plain_path = tma ? 1 : 0;
-    info->autotune_us[0] = ctx->autotune_us[0];
-    info->autotune_us[1] = ctx->autotune_us[1];
+    bool use8 = false;
+    for (auto &l : ctx->lv) use8 |= l.use8;
+    info->plain_path = use8 ? 2 : tma ? 1 : 0;
+    for (int k = 0; k < 3; k++) info->autotune_us[k] = ctx->autotune_us[k];
     return MGPU_OK;
 }
 
@@ -1310,8 +1390,7 @@ int mgpu_step_level(mgpu_ctx *ctx, int level, int n)
         for (int i = 0; i < n; i++)
         {
             PhaseVariant &V = plan_variant(P, {ctx}, 0);
-            launch_phase(V.plain[0], V.tma[0], V.spec[0], none, ctx->stream, ctx->side_stream, ctx->ev_fork,
-                         ctx->ev_join, ctx->launches);
+            launch_phase(V, 0, none, ctx->stream, ctx->lanes, ctx->launches);
             ctx->lv[l].steps++;
         }
         return MGPU_OK;
@@ -1628,9 +1707,16 @@ struct mgpu_batch
 {
     std::vector<mgpu_ctx *> ctxs;
     std::unique_ptr<PhasePlan> plan;
-    cudaStream_t stream = nullptr, side = nullptr;
+    cudaStream_t stream = nullptr;
+    SideLanes lanes;
     bool own_stream = false;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_done = nullptr;
+    // images step concurrently, each on its own stream (with its own side
+    // lanes), forked from and joined back to `stream` around their coarse steps
+    std::vector<cudaStream_t> img_stream;
+    std::vector<SideLanes> img_lanes;
+    std::vector<cudaEvent_t> img_done;
+    cudaEvent_t ev_start = nullptr;
     std::vector<cudaEvent_t> ctx_ev;
     cudaGraphExec_t graph = nullptr;
     std::string graph_key;
@@ -1657,10 +1743,29 @@ void batch_leave(mgpu_batch *b)
         if (c->stream != b->stream) CK(cudaStreamWaitEvent(c->stream, b->ev_done, 0));
 }
 
-void batch_step(mgpu_batch *b)
+// n coarse steps of every image: each image on its own stream with its own
+// phase launches, so that one image's small launches (interface waves, the
+// sparse coarse levels) overlap another's; images share no data
+void batch_step(mgpu_batch *b, int n = 1)
 {
-    phase_step(*b->plan, b->ctxs, b->stream, b->side, b->ev_fork, b->ev_join, dev::PhaseArgs{0, 0, 0}, b->launches);
-    for (auto *c : b->ctxs) c->ref_t++;
+    const dev::PhaseArgs none{0, 0, 0};
+    if (b->img_stream.empty())
+    {
+        for (int k = 0; k < n; k++) phase_step(*b->plan, b->ctxs, b->stream, b->lanes, none, b->launches);
+    }
+    else
+    {
+        CK(cudaEventRecord(b->ev_start, b->stream));
+        for (size_t i = 0; i < b->ctxs.size(); i++)
+        {
+            CK(cudaStreamWaitEvent(b->img_stream[i], b->ev_start, 0));
+            for (int k = 0; k < n; k++)
+                phase_step(*b->ctxs[i]->plan, {b->ctxs[i]}, b->img_stream[i], b->img_lanes[i], none, b->launches);
+            CK(cudaEventRecord(b->img_done[i], b->img_stream[i]));
+            CK(cudaStreamWaitEvent(b->stream, b->img_done[i], 0));
+        }
+    }
+    for (auto *c : b->ctxs) c->ref_t += n;
 }
 } // namespace
 
@@ -1686,10 +1791,21 @@ int mgpu_batch_create(mgpu_ctx *const *ctxs, int n, mgpu_batch **out)
         b->plan = build_plan(b->ctxs, -1);
         CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
         b->own_stream = true;
-        CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+        b->lanes.create();
         CK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
+        if (b->ctxs.size() > 1)
+        {
+            CK(cudaEventCreateWithFlags(&b->ev_start, cudaEventDisableTiming));
+            b->img_stream.resize(b->ctxs.size());
+            b->img_lanes.resize(b->ctxs.size());
+            b->img_done.resize(b->ctxs.size());
+            for (size_t i = 0; i < b->ctxs.size(); i++)
+            {
+                CK(cudaStreamCreateWithFlags(&b->img_stream[i], cudaStreamNonBlocking));
+                b->img_lanes[i].create();
+                CK(cudaEventCreateWithFlags(&b->img_done[i], cudaEventDisableTiming));
+            }
+        }
         b->ctx_ev.resize(b->ctxs.size());
         for (auto &e : b->ctx_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         *out = b.release();
@@ -1722,6 +1838,11 @@ int mgpu_batch_advance(mgpu_batch *b, int n_steps)
             // two coarse steps: every level of every image returns to its parity
             plan_variant(*b->plan, b->ctxs, 0);
             plan_variant(*b->plan, b->ctxs, 1);
+            for (auto *c : b->ctxs)
+            {
+                plan_variant(*c->plan, {c}, 0);
+                plan_variant(*c->plan, {c}, 1);
+            }
             b->graph_key = state_key(b->ctxs, 0);
             std::vector<std::vector<int64_t>> saved;
             std::vector<int64_t> saved_done, saved_t;
@@ -1735,8 +1856,7 @@ int mgpu_batch_advance(mgpu_batch *b, int n_steps)
             const int64_t l0 = b->launches;
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            batch_step(b);
-            batch_step(b);
+            batch_step(b, 2);
             CK(cudaStreamEndCapture(b->stream, &g));
             CK(cudaGraphInstantiate(&b->graph, g, 0));
             CK(cudaGraphDestroy(g));
@@ -1838,11 +1958,19 @@ int mgpu_batch_destroy(mgpu_batch *b)
 {
     if (!b) return MGPU_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->side) cudaStreamSynchronize(b->side);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->side) cudaStreamDestroy(b->side);
-    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
-    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    b->lanes.destroy();
+    for (size_t i = 0; i < b->img_stream.size(); i++)
+    {
+        if (b->img_stream[i])
+        {
+            cudaStreamSynchronize(b->img_stream[i]);
+            cudaStreamDestroy(b->img_stream[i]);
+        }
+        b->img_lanes[i].destroy();
+        if (b->img_done[i]) cudaEventDestroy(b->img_done[i]);
+    }
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->ev_done) cudaEventDestroy(b->ev_done);
     for (auto e : b->ctx_ev) cudaEventDestroy(e);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);

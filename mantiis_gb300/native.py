@@ -57,7 +57,7 @@ class Info(C.Structure):
         ("grid_undefined_cases", C.c_int64),
         ("plain_path", C.c_int),
         ("pad_", C.c_int),
-        ("autotune_us", C.c_double * 2),
+        ("autotune_us", C.c_double * 3),
     ]
 
 

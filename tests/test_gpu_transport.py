@@ -193,20 +193,22 @@ def test_collision_and_wall_variants_vs_oracle(fixture64, collision, wall, multi
 
 
 def test_plain_paths_agree_and_autotune():
-    # the TMA pipeline and the direct loads run the same arithmetic on the same
-    # slots: bit-identical states; plain_path -1 times both and keeps one
+    # the TMA pipeline, the direct 32x8 tiles and the direct 8x4 warp tiles run
+    # the same arithmetic on the same slots: bit-identical states; plain_path -1
+    # times all three and keeps the fastest
     pore = generate_disks(256, 6, 20, 0.6, 77, open_x_edges=True)
     kn = np.where(pore == 1, 0.1, 0.0)
     lp = np.where(pore == 1, 7.73, 0.0)
     runs = {}
-    for path in (0, 1, -1):
+    for path in (0, 1, 2, -1):
         s = Solver(pore, kn, lp, default_params(plain_path=path, multiblock=1, edge_fine=1))
         s.advance(20)
         runs[path] = (s.cells(with_f=True)["f"], s.info)
-    assert runs[1][1]["plain_path"] == 1 and runs[0][1]["plain_path"] == 0
+    assert [runs[k][1]["plain_path"] for k in (0, 1, 2)] == [0, 1, 2]
     assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][0], runs[2][0])
     assert np.array_equal(runs[0][0], runs[-1][0])
     us = runs[-1][1]["autotune_us"]
-    assert us[0] > 0 and us[1] > 0
-    assert runs[-1][1]["plain_path"] == (1 if us[1] < us[0] else 0)
-    record("autotune_256", direct_us=us[0], tma_us=us[1])
+    assert min(us) > 0
+    assert runs[-1][1]["plain_path"] == int(np.argmin(us))
+    record("autotune_256", direct_us=us[0], tma_us=us[1], direct8x4_us=us[2])
