@@ -58,26 +58,39 @@ class ClockSampler:
         self._th = None
 
     def start(self):
+        # one nvidia-smi in loop mode (a sample every 50 ms), read line by line
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+
         def run():
-            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
-                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap")
-            while not self._stop.is_set():
-                try:
-                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                         timeout=5).stdout.strip()
-                    if out:
-                        self.rows.append([v.strip() for v in out.split(",")])
-                except Exception:
-                    pass
-                self._stop.wait(0.2)
+            for line in self._proc.stdout:
+                if self._stop.is_set():
+                    break
+                line = line.strip()
+                if line:
+                    self.rows.append([v.strip() for v in line.split(",")])
 
         self._th = threading.Thread(target=run, daemon=True)
         self._th.start()
+        time.sleep(0.3)  # nvidia-smi is up and sampling before the timed region starts
+        self.rows.clear()
 
     def stop(self):
         self._stop.set()
+        if getattr(self, "_proc", None) is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
         if self._th:
             self._th.join(timeout=10)
         if not self.rows:
@@ -188,7 +201,7 @@ def run_properties(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--images", type=int, default=4)

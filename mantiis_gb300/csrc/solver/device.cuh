@@ -22,7 +22,9 @@ namespace dev
 {
 // boundary tables in constant memory: specular target per (type, direction),
 // and per type the directions with c.n > 0 and c.n < 0 (MDBB)
-__constant__ unsigned char c_icsr[MANTIIS_N_BND_TYPES * 9];
+// specular targets per boundary type, in global memory: lanes of a warp index it
+// with different types, which the constant cache would serialize
+__device__ unsigned char c_icsr[MANTIIS_N_BND_TYPES * 9];
 __constant__ unsigned short c_npos[MANTIIS_N_BND_TYPES];
 __constant__ unsigned short c_nneg[MANTIIS_N_BND_TYPES];
 struct LevelView
@@ -352,41 +354,56 @@ __device__ __forceinline__ void special_rules(const Common &C, const SpecialRec 
 {
     const uint32_t arrive = rec.m0 & 0x1FFu, over = (rec.m0 >> 9) & 0x1FFu, wall = (rec.m0 >> 18) & 0x1FFu;
     const uint32_t quirk = rec.m1 & 0x1FFu, bnd = (rec.m1 >> 9) & 0xFFu, flags = (rec.m1 >> 17) & 0xFu;
+    // every load first (wall values, quirk values, constant terms, specular
+    // targets), so they are in flight together; then the arithmetic in the
+    // reference's order
+    const float *side_prev = C.side + (size_t)(P ^ 1) * C.n_quirk;
+    float v[9], kq[9];
+    int p2s[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+    {
+        v[q] = 0.0f;
+        p2s[q] = d2q9::opp(q);
+        if ((wall >> q) & 1u)
+        {
+            v[q] = ((quirk >> q) & 1u) ? side_prev[rec.quirk_base + __popc(quirk & ((1u << q) - 1u))] : wall_of(q);
+            if (bnd != 0xFFu) p2s[q] = (int)__ldg(&c_icsr[bnd * 9 + q]);
+        }
+    }
+    const bool has_k = (flags & SF_HAS_K) != 0;
+    const float *k = C.ktab + (size_t)(has_k ? rec.k_row : 0) * 9;
+#pragma unroll
+    for (int q = 0; q < 9; q++) kq[q] = has_k ? __ldg(&k[q]) : 0.0f;
 #pragma unroll
     for (int q = 0; q < 9; q++) df[q] = ((arrive >> q) & 1u) ? raw[q] : 0.0f;
     if (wall)
     {
         const float r = rec.r;
-        int qi = 0;
-        const float *side_prev = C.side + (size_t)(P ^ 1) * C.n_quirk;
         // unrolled with fixed indices (the specular target is matched against
         // each population), so df stays in registers
 #pragma unroll
         for (int q = 0; q < 9; q++)
         {
             if (!((wall >> q) & 1u)) continue;
-            float v;
-            if ((quirk >> q) & 1u) v = side_prev[rec.quirk_base + qi++];
-            else v = wall_of(q);
             const int p1 = d2q9::opp(q);
             if (C.wall == WALL_SRBB)
             {
-                const int p2 = (bnd == 0xFFu) ? p1 : (int)c_icsr[bnd * 9 + q];
-                if (!((over >> p1) & 1u)) df[p1] += r * v;
-                const float rv = (((over >> p2) & 1u) ? 0.0f : (1.0f - r) * v);
+                const int p2 = p2s[q];
+                if (!((over >> p1) & 1u)) df[p1] += r * v[q];
+                const float rv = (((over >> p2) & 1u) ? 0.0f : (1.0f - r) * v[q]);
 #pragma unroll
                 for (int p = 0; p < 9; p++)
                     if (p == p2) df[p] += rv;
             }
             else if (!((over >> p1) & 1u))
-                df[p1] = v;
+                df[p1] = v[q];
         }
     }
-    if (flags & SF_HAS_K)
+    if (has_k)
     {
-        const float *k = C.ktab + (size_t)rec.k_row * 9;
 #pragma unroll
-        for (int q = 0; q < 9; q++) df[q] += k[q];
+        for (int q = 0; q < 9; q++) df[q] += kq[q];
     }
     if ((flags & SF_INLET) && C.inlet_outlet)
     {

@@ -704,31 +704,54 @@ __device__ __forceinline__ void store_for_load(const LevelView &L, int x, int y,
     }
 }
 
+// The interface rows are handled by groups of 4 adjacent lanes (lane & 3 = k):
+// each lane loads one child (coarse rows) or one or two spline nodes (fine
+// rows), and the group exchanges the loaded populations with shuffles, so the
+// loads of a row are in flight together and each is made once.  Sums run in
+// the same order as one lane summing alone.
+
+// populations of an interface source cell: its interpolation buffer, or the
+// cell's own slots after streaming and its rules
+template <int P>
+__device__ __forceinline__ void load_source(const LevelView &L, const Common &C, int site, int buf, float z[9])
+{
+    if (buf >= 0)
+    {
+#pragma unroll
+        for (int q = 0; q < 9; q++) z[q] = C.ibuf[(size_t)q * C.n_buf + buf];
+    }
+    else
+    {
+        bool special;
+        SpecialRec rec;
+        load_cell<P>(L, C, site % L.pitch, site / L.pitch, 0, 0, z, special, rec);
+    }
+}
+
 // Coarse buffer cells <- rescaled mean of their 4 children
 // (include/coreLB.hpp:1104-1135): f_c = f_eq,c + 2 tau_c / mean(tau_f) (mean(f_f) - f_eq,c).
+// Lane k of the group loads child k; lane 0 writes the result.
 template <int PF>
 __device__ __forceinline__ void coarse_row(const LevelView &Lf, const LevelView &Lc, const Common &C,
-                                           const CoarseRowDev &row, int pc)
+                                           const CoarseRowDev &row, int k, bool valid, int pc)
 {
+    const int lane = threadIdx.x & 31, base = lane & ~3;
+    const bool has = valid && row.child[k] >= 0;
+    float df[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (has) load_source<PF>(Lf, C, row.child[k], row.child_buf[k], df);
     float mean[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++)
     {
-        if (row.child[k] < 0) continue;
-        float df[9];
-        if (row.child_buf[k] >= 0)
-        {
+        const bool present = __shfl_sync(0xffffffffu, has ? 1 : 0, base + kk) != 0;
 #pragma unroll
-            for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + row.child_buf[k]];
-        }
-        else
+        for (int q = 0; q < 9; q++)
         {
-            bool special;
-            SpecialRec rec;
-            load_cell<PF>(Lf, C, row.child[k] % Lf.pitch, row.child[k] / Lf.pitch, 0, 0, df, special, rec);
+            const float v = __shfl_sync(0xffffffffu, df[q], base + kk);
+            if (present) mean[q] += v;
         }
-#pragma unroll
-        for (int q = 0; q < 9; q++) mean[q] += df[q];
     }
+    if (!valid || k != 0) return;
     const float drho = Lc.snap[row.site], ux = Lc.snap[Lc.plane + row.site], uy = Lc.snap[2 * Lc.plane + row.site];
     float feq[9];
     equilibrium(drho, C.rho0 + drho, ux, uy, feq);
@@ -745,32 +768,31 @@ __device__ __forceinline__ void coarse_row(const LevelView &Lf, const LevelView 
 // Fine buffer cells <- bicubic spline of the parent neighbourhood
 // (include/coreLB.hpp:1137-1230); the spline is linear in the node values, so
 // each child holds 6 precomputed weights.  f = f_eq + tau_f / (2 tau_c) (f_spline - f_eq).
+// Lane c of the group loads nodes c and c + 4 (c < 2) and computes child c.
 template <int PC>
 __device__ __forceinline__ void fine_child(const LevelView &Lf, const LevelView &Lc, const Common &C,
-                                           const FineRowDev &row, int c, int pf)
+                                           const FineRowDev &row, int c, bool valid, int pf)
 {
+    const int lane = threadIdx.x & 31, base = lane & ~3;
+    float za[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, zb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (valid)
+    {
+        load_source<PC>(Lc, C, row.node_site[c], row.node_buf[c], za);
+        if (c < 2) load_source<PC>(Lc, C, row.node_site[c + 4], row.node_buf[c + 4], zb);
+    }
     float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < 6; k++)
     {
-        float z[9];
-        const int nb = row.node_buf[k];
-        if (nb >= 0)
-        {
+        const float w = valid ? row.weight[c][k] : 0.0f;
 #pragma unroll
-            for (int q = 0; q < 9; q++) z[q] = C.ibuf[(size_t)q * C.n_buf + nb];
-        }
-        else
+        for (int q = 0; q < 9; q++)
         {
-            bool special;
-            SpecialRec rec;
-            const int ns = row.node_site[k];
-            load_cell<PC>(Lc, C, ns % Lc.pitch, ns / Lc.pitch, 0, 0, z, special, rec);
+            const float z = __shfl_sync(0xffffffffu, k < 4 ? za[q] : zb[q], base + (k & 3));
+            acc[q] += w * z;
         }
-        const float w = row.weight[c][k];
-#pragma unroll
-        for (int q = 0; q < 9; q++) acc[q] += w * z[q];
     }
+    if (!valid) return;
     const int s = row.child_site[c];
     const float drho = Lf.snap[s], ux = Lf.snap[Lf.plane + s], uy = Lf.snap[2 * Lf.plane + s];
     float feq[9];
@@ -785,6 +807,7 @@ __device__ __forceinline__ void fine_child(const LevelView &Lf, const LevelView 
     }
     if ((row.plain_mask >> c) & 1) store_for_load(Lf, s % Lf.pitch, s / Lf.pitch, acc, pf);
 }
+
 
 // One level pair of one image in the interface exchange: the two levels'
 // states (at their parities after the coarse step) and the pair's rows.
@@ -809,28 +832,27 @@ struct WaveLaunch
 };
 
 // Interface exchange wave: coarse rows of some pairs and fine rows of others
-// (independent within a wave), 128 coarse rows or 32 fine rows (128 children) per block.
+// (independent within a wave), 32 rows per block, 4 lanes per row.
 __global__ void __launch_bounds__(128) k_wave(const __grid_constant__ WaveLaunch W)
 {
     const int j = owner(W.start, W.ndesc, (int)blockIdx.x);
     const PairDesc &d = W.d[j];
     const int u = ((int)blockIdx.x - W.start[j]) * 128 + (int)threadIdx.x;
+    const int r = u >> 2, k = u & 3;
+    // lanes past the last row stay for the group shuffles
+    const bool valid = r < d.nrows;
+    const int rr = valid ? r : 0;
     if (d.kind == 0)
     {
-        // one thread per coarse row
-        if (u >= d.nrows) return;
-        const CoarseRowDev row = d.coarse[u];
-        if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row, d.pc);
-        else coarse_row<0>(d.Lf, d.Lc, d.C, row, d.pc);
+        const CoarseRowDev &row = d.coarse[rr];
+        if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row, k, valid, d.pc);
+        else coarse_row<0>(d.Lf, d.Lc, d.C, row, k, valid, d.pc);
     }
     else
     {
-        // one thread per fine child (4 per row)
-        const int r = u >> 2, c = u & 3;
-        if (r >= d.nrows) return;
-        const FineRowDev &row = d.fine[r];
-        if (d.pc) fine_child<1>(d.Lf, d.Lc, d.C, row, c, d.pf);
-        else fine_child<0>(d.Lf, d.Lc, d.C, row, c, d.pf);
+        const FineRowDev &row = d.fine[rr];
+        if (d.pc) fine_child<1>(d.Lf, d.Lc, d.C, row, k, valid, d.pf);
+        else fine_child<0>(d.Lf, d.Lc, d.C, row, k, valid, d.pf);
     }
 }
 

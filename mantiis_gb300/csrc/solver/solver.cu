@@ -808,7 +808,7 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
         {
             d.kind = 0;
             d.nrows = it.ncoarse;
-            wv[it.l1 - 1].push_back({d, (it.ncoarse + 127) / 128});
+            wv[it.l1 - 1].push_back({d, (it.ncoarse + 31) / 32});
         }
         if (it.nfine)
         {
