@@ -118,12 +118,13 @@ def make_images(count, offset, workload="config2"):
     return [dict(workloads.config2(offset + i), levels=3) for i in range(count)]
 
 
-def params_for(img):
+def params_for(img, plain_path=-1):
     from mantiis_gb300 import default_params
 
     if img.get("levels", 3) == 1:
-        return default_params(multiblock=0, dx=img["dx"])
-    return default_params(multiblock=1, max_allowed_level=img["levels"], dx=img["dx"], edge_fine=1)
+        return default_params(multiblock=0, dx=img["dx"], plain_path=plain_path)
+    return default_params(multiblock=1, max_allowed_level=img["levels"], dx=img["dx"], edge_fine=1,
+                          plain_path=plain_path)
 
 
 def cpu_oracle_rate(img, seconds, threads):
@@ -211,6 +212,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--properties", type=int, default=0, metavar="N")
+    # plain-cell kernels: -1 times all three at creation (autotune); a fixed
+    # path keeps profiled runs, whose timings the profiler distorts, on one path
+    ap.add_argument("--plain-path", type=int, default=-1, choices=[-1, 0, 1, 2])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -242,7 +246,7 @@ def main():
     assert stream.cuda_stream != 0
     solvers = []
     for img in imgs:
-        s = Solver(img["pore"], img["kn"], img["locpore"], params_for(img))
+        s = Solver(img["pore"], img["kn"], img["locpore"], params_for(img, args.plain_path))
         s.set_stream(stream.cuda_stream)
         solvers.append(s)
     lu_step = float(sum(s.info["lu_per_step"] for s in solvers))
@@ -280,7 +284,7 @@ def main():
     batch.close()
 
     # roofline: finest-level step kernel of image 0 on a separate context
-    prof = Solver(imgs[0]["pore"], imgs[0]["kn"], imgs[0]["locpore"], params_for(imgs[0]))
+    prof = Solver(imgs[0]["pore"], imgs[0]["kn"], imgs[0]["locpore"], params_for(imgs[0], args.plain_path))
     prof.set_stream(stream.cuda_stream)
     prof.advance(2)
     lvl1 = prof.level_info(1)
