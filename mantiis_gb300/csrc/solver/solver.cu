@@ -203,6 +203,7 @@ struct mgpu_ctx
     DevBuf<float> ktab, side, ibuf;
     DevBuf<int32_t> cell_level, cell_site;
     DevBuf<double> red;     // kRing * 4
+    double *red_host = nullptr; // pinned staging copy of the accumulators
     DevBuf<double> out_rho, out_ux, out_uy, out_f;
     DevBuf<unsigned int> errword;
     float rho0f = 0.f;
@@ -512,11 +513,36 @@ void cells_pass(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f, b
 void zero_slots(mgpu_ctx *ctx, int first, int count)
 {
     // slots are used cyclically; zero a contiguous (possibly wrapping) range
-    for (int k = 0; k < count; k++)
+    // with at most two calls
+    first %= kRing;
+    count = std::min(count, kRing);
+    const int a = std::min(count, kRing - first);
+    if (a > 0) CK(cudaMemsetAsync(ctx->red.p + (size_t)first * 4, 0, (size_t)a * 4 * sizeof(double), ctx->stream));
+    if (count > a) CK(cudaMemsetAsync(ctx->red.p, 0, (size_t)(count - a) * 4 * sizeof(double), ctx->stream));
+}
+
+// the accumulators of `count` consecutive slots from `first` (wrapping) into
+// out[4 * count]: at most two copies into the context's pinned staging array,
+// then a wait on the stream
+void read_slots(mgpu_ctx *ctx, int first, int count, double *out)
+{
+    first %= kRing;
+    if (count <= 0) return;
+    if (count > kRing) throw std::logic_error("read_slots: more slots than the ring holds");
+    if (!ctx->red_host)
     {
-        int s = (first + k) % kRing;
-        CK(cudaMemsetAsync(ctx->red.p + (size_t)s * 4, 0, 4 * sizeof(double), ctx->stream));
+        void *p = nullptr;
+        CK(cudaMallocHost(&p, (size_t)kRing * 4 * sizeof(double)));
+        ctx->red_host = static_cast<double *>(p);
     }
+    const int a = std::min(count, kRing - first);
+    CK(cudaMemcpyAsync(ctx->red_host, ctx->red.p + (size_t)first * 4, (size_t)a * 4 * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    if (count > a)
+        CK(cudaMemcpyAsync(ctx->red_host + (size_t)a * 4, ctx->red.p, (size_t)(count - a) * 4 * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::copy(ctx->red_host, ctx->red_host + (size_t)count * 4, out);
 }
 
 void read_slot(mgpu_ctx *ctx, int slot, double out[4])
@@ -1180,6 +1206,7 @@ int mgpu_destroy(mgpu_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->lanes.destroy();
+    if (ctx->red_host) cudaFreeHost(ctx->red_host);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MGPU_OK;
@@ -1233,8 +1260,7 @@ int mgpu_run(mgpu_ctx *ctx, int n_steps, int *steps_done)
             int64_t k0 = ctx->coarse_done;
             run_batch_with_residuals(ctx, batch);
             std::vector<double> slots((size_t)batch * 4);
-            for (int i = 0; i < batch; i++) read_slot(ctx, (int)((k0 + 1 + i) % kRing), &slots[(size_t)i * 4]);
-            CK(cudaStreamSynchronize(ctx->stream));
+            read_slots(ctx, (int)((k0 + 1) % kRing), batch, slots.data());
             int stop = -1;
             for (int i = 0; i < batch; i++)
             {
