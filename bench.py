@@ -59,13 +59,13 @@ class ClockSampler:
         self._th = None
 
     def start(self):
-        # one nvidia-smi in loop mode (a sample every 50 ms), read line by line
+        # one nvidia-smi in loop mode (a sample every 25 ms), read line by line
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
             self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                           "--format=csv,noheader,nounits", "-lms", "25"],
                                           stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self._proc = None
@@ -149,26 +149,57 @@ def cpu_oracle_rate(img, seconds, threads):
     return lu * steps / dt / 1e6, steps, dt, lu
 
 
+def job_rate(lu_local, ms_local, steps, dist=None, device="cpu"):
+    """Whole-job MLUPS over all ranks (weak scaling: every rank steps its own
+    images): the lattice updates of all ranks over the slowest rank's time.
+    Returns (MLUPS, max ms, lattice updates per step of the job)."""
+    ms, lu = float(ms_local), float(lu_local)
+    if dist:
+        import torch
+
+        t_ms = torch.tensor([ms], dtype=torch.float64, device=device)
+        t_lu = torch.tensor([lu], dtype=torch.float64, device=device)
+        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t_lu, op=dist.ReduceOp.SUM)
+        ms, lu = float(t_ms.item()), float(t_lu.item())
+    return lu * steps / (ms / 1e3) / 1e6, ms, lu
+
+
 def run_reference(args, rank, world):
+    """The CPU arm: the FP64 oracle restatement of the reference step on all host
+    cores.  A step is one sample of n coarse steps of image 0, n sized so that the
+    whole run (warm-up and K samples) stays within about --ref-budget seconds."""
     if rank != 0:
         return
+    from mantiis_gb300 import HostGrid
+    from oracle.pyoracle import for_grid
+
     img = make_images(1, 0)[0]
     threads = os.cpu_count() or 1
-    samples = []
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], params_for(img))
+    lu = float(np.sum([(1 << (g.max_level - l)) for l, b in zip(g.cells["level"], g.cells["is_buffer"]) if not b]))
+    o = for_grid(g, sim="transport", dx=img["dx"], threads=threads)
+    t0 = time.perf_counter()
+    o.run(1)
+    per = max(time.perf_counter() - t0, 1e-6)
+    n = max(1, int(args.ref_budget / ((args.steps + args.warmup) * per)))
     for _ in range(args.warmup):
-        cpu_oracle_rate(img, 2.0, threads)
+        o.run(n)
+    rates = []
     for _ in range(args.steps):
-        samples.append(cpu_oracle_rate(img, args.ref_seconds, threads))
-    rate = float(np.median([s[0] for s in samples]))
-    steps = samples[-1][1]
+        t0 = time.perf_counter()
+        o.run(n)
+        rates.append(lu * n / (time.perf_counter() - t0) / 1e6)
+    o.close()
+    rate = float(np.median(rates))
     line = {
         "impl": "reference", "metric": "MLUPS", "value": rate, "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "images": 1, "n": 1024, "levels": 3},
         "cpu_baseline": {"value": rate, "unit": "MLUPS", "cores": threads, "kind": "port",
-                         "sample": f"1 image, {steps} coarse steps per measurement, FP64 oracle restatement "
-                                   f"of the reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads"},
+                         "sample": f"image 0, {n} coarse step(s) per step (median of {args.steps}), FP64 oracle "
+                                   f"restatement of the reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads"},
         "e2e": {"value": rate, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -203,12 +234,12 @@ def run_properties(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--images", type=int, default=4)
     ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
@@ -275,11 +306,7 @@ def main():
     clocks = clk.stop()
     ms = e0.elapsed_time(e1)
     launches = batch.launches - l0
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = lu_step * world * K / (ms / 1e3) / 1e6
+    value, ms, lu_job = job_rate(lu_step, ms, K, dist, "cuda")
 
     finite = all(np.isfinite(o["mean_ux"]) for o in batch.observables())
     batch.close()
