@@ -205,6 +205,55 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_adsorption(args):
+    """Config 3 (Shan-Chen adsorption, 512x512 seeded disk image, porosity 0.6,
+    psi = rho0 (1 - exp(-rho/rho0)), G = -4.5, G_ads = -0.5, rho = 0.5 +- 1e-3):
+    MLUPS of the two-pass adsorption step with the per-step density residual,
+    device-timed over K steps, and the roofline of the step (80 B per update:
+    72 B of populations and the psi plane written and read)."""
+    import torch
+
+    from mantiis_gb300 import SIM_ADSORPTION, Solver, default_params
+    from mantiis_gb300.workloads import config3
+
+    img = config3(0)
+    # the common-convention constants in the reference's force convention
+    p = default_params(dx=img["dx"], simulation=SIM_ADSORPTION, rho_init=0.5, fbody=0.0, psi_form=1, rho_psi=0.5,
+                       g_ff=-4.5 / 18, g_fs=3 * -0.5, check_every=1)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    s.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(3000)
+    rho = 0.5 + rng.uniform(-1e-3, 1e-3, s.n_cells)
+    s.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
+    s.advance(args.warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.advance(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = s.info["lu_per_step"]
+    mass = float(s.observables()["mass"])
+    s.close()
+    peak, peak_kind = peaks()
+    achieved = 80.0 * cells * args.steps / (ms / 1e3) / 1e9
+    print(json.dumps({
+        "metric": "MLUPS", "value": cells * args.steps / (ms / 1e3) / 1e6, "unit": "MLUPS", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "config3: 512x512 seeded disk image, porosity 0.6, Shan-Chen adsorption, "
+                               "exponential psi (rho0 0.5), G -4.5, G_ads -0.5, rho 0.5 +- 1e-3",
+                   "cells": cells, "l2": "state L2-resident (one 512^2 image)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "adsorption step (k_ads_psi + k_ads_step)",
+                     "bytes_per_unit": 80.0},
+        "mass_after": mass,
+    }))
+
+
 def run_properties(args):
     from mantiis_gb300 import generate_disks, pore_properties, pore_properties_gpu
 
@@ -244,6 +293,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--properties", type=int, default=0, metavar="N")
+    ap.add_argument("--adsorption", action="store_true", help="time the config-3 adsorption step instead")
     # plain-cell kernels: -1 times all three at creation (autotune); a fixed
     # path keeps profiled runs, whose timings the profiler distorts, on one path
     ap.add_argument("--plain-path", type=int, default=-1, choices=[-1, 0, 1, 2])
@@ -257,6 +307,9 @@ def main():
         return
     if args.properties:
         run_properties(args)
+        return
+    if args.adsorption:
+        run_adsorption(args)
         return
 
     import torch

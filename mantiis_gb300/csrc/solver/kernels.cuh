@@ -524,9 +524,10 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, C
 // the same body with the regularized MRT, SRBB walls, no inlet / outlet and the
 // velocity residual (C.collision, C.wall, C.inlet_outlet; o.diff accumulates
 // sum |u| for both terms, as its |u| of the previous step is never stored).
+// psi[r][c]: the pseudopotential at (x + c - 1, y + r - 1)
 template <int P>
 __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y,
-                                         double &r_diff, double &r_norm)
+                                         const float psi[3][3], double &r_diff, double &r_norm)
 {
     const int64_t s = site_of(L, x, y);
     float df[9];
@@ -536,7 +537,7 @@ __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, co
     const uint32_t out = special ? ((rec.m1 >> 21) & 0x1FFu) : 0x1FFu;
     const uint32_t wall = special ? ((rec.m0 >> 18) & 0x1FFu) : 0u;
     // sum over the streaming links of w_f psi(x + c) c, formed from psi differences
-    const float psx = L.psi[s];
+    const float psx = psi[1][1];
     float sx = 0.f, sy = 0.f, cwx = 0.f, cwy = 0.f, wwx = 0.f, wwy = 0.f;
 #pragma unroll
     for (int q = 1; q < 9; q++)
@@ -544,8 +545,7 @@ __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, co
         const float w = (float)d2q9::wf(q);
         if ((out >> q) & 1u)
         {
-            const int xn = wrapx(x + d2q9::cx(q), L.W), yn = wrapx(y + d2q9::cy(q), L.H);
-            const float dpsi = L.psi[site_of(L, xn, yn)] - psx;
+            const float dpsi = psi[1 + d2q9::cy(q)][1 + d2q9::cx(q)] - psx;
             sx += w * dpsi * (float)d2q9::cx(q);
             sy += w * dpsi * (float)d2q9::cy(q);
             cwx += w * (float)d2q9::cx(q);
@@ -600,13 +600,30 @@ __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, co
     store_post<P>(L, x, y, fs);
 }
 
+// The neighbour pseudopotentials come by warp shuffles: a warp holds one row of
+// a 32x8 tile, each lane loads psi of its column in the rows y-1, y, y+1
+// (coalesced), and takes the x-neighbours from the adjacent lanes; the lanes at
+// the ends of the row (and the last image column) load their outer neighbours.
 template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
 {
     const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
-    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
+    const int lane = threadIdx.x & 31;
+    const int x = (tile & 0xFFFF) * 32 + lane;
     const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
+    const bool inside = x < L.W && y < L.H;
+    float psi[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+    {
+        const int yr = wrapx(y + r - 1, L.H);
+        psi[r][1] = inside ? L.psi[site_of(L, x, yr)] : 0.0f;
+        psi[r][0] = __shfl_up_sync(0xffffffffu, psi[r][1], 1);
+        psi[r][2] = __shfl_down_sync(0xffffffffu, psi[r][1], 1);
+        if (inside && lane == 0) psi[r][0] = L.psi[site_of(L, wrapx(x - 1, L.W), yr)];
+        if (inside && (lane == 31 || x + 1 == L.W)) psi[r][2] = L.psi[site_of(L, wrapx(x + 1, L.W), yr)];
+    }
     double r_diff = 0.0, r_norm = 0.0;
-    if (x < L.W && y < L.H && L.omega[site_of(L, x, y)] != 0.0f) ads_cell<P>(L, C, o, x, y, r_diff, r_norm);
+    if (inside && L.omega[site_of(L, x, y)] != 0.0f) ads_cell<P>(L, C, o, x, y, psi, r_diff, r_norm);
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 
