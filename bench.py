@@ -400,22 +400,33 @@ def main():
     for s, st in zip(solvers, e2e_streams):
         s.set_stream(st.cuda_stream)
 
-    def e2e_image(s, steps):
+    # pinned host buffers per image: the initial state and the fields read back
+    pinned = []
+    for s in solvers:
         n = s.n_cells
-        rho = np.full(n, s.info["rho_in"])
-        z = np.zeros(n)
-        s.set_equilibrium(rho, z, z)
+        buf = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+               for k in ("rho", "ux", "uy", "out_rho", "out_ux", "out_uy")}
+        buf["rho"][:] = s.info["rho_in"]
+        buf["ux"][:] = 0.0
+        buf["uy"][:] = 0.0
+        pinned.append(buf)
+
+    def e2e_image(i, steps):
+        s, b = solvers[i], pinned[i]
+        n = s.n_cells
+        s.set_equilibrium(b["rho"], b["ux"], b["uy"])
         s.run(steps)
-        s.cells()
+        s.cells(out={"rho": b["out_rho"], "ux": b["out_ux"], "uy": b["out_uy"]})
         return 3 * n * 8, 3 * n * 8 + steps * 4 * 8
 
     from concurrent.futures import ThreadPoolExecutor
 
     with ThreadPoolExecutor(len(solvers)) as ex:
-        list(ex.map(lambda s: e2e_image(s, 2), solvers))  # untimed: plans and checkpoint buffers
+        # untimed: plans, checkpoint buffers and the two-step residual graph
+        list(ex.map(lambda i: e2e_image(i, 5), range(len(solvers))))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        moved = list(ex.map(lambda s: e2e_image(s, Ke), solvers))
+        moved = list(ex.map(lambda i: e2e_image(i, Ke), range(len(solvers))))
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
     h2d = sum(m[0] for m in moved)

@@ -490,27 +490,55 @@ __device__ __forceinline__ void block_max(double v, double *dst)
 // include/coreLB.hpp:1056-1067, 515-531, 1269-1283): density of every cell from
 // its streamed populations, its pseudopotential, and the relative density change
 // since the previous step (maximum over the cells).
-template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
+// density and pseudopotential of one cell (pass 1), the density change against
+// the previous step's density for the residual
+template <int P, bool SPEC>
+__device__ __forceinline__ double ads_density(const LevelView &L, const Common &C, const StepOpt &o, int x, int y)
 {
-    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
-    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
-    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
-    double rmax = 0.0;
-    if (x < L.W && y < L.H && L.omega[site_of(L, x, y)] != 0.0f)
+    const int64_t s = site_of(L, x, y);
+    float df[9];
+    if (SPEC)
     {
-        const int64_t s = site_of(L, x, y);
-        float df[9];
         bool special;
         SpecialRec rec;
         load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
-        float drho = 0.0f;
+    }
+    else if (o.direct)
+        load_raw<0>(L, x, y, df);
+    else
+        load_raw<P>(L, x, y, df);
+    float drho = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 9; q++) drho += df[q];
-        const float rho = C.rho0 + drho;
-        L.psi[s] = pseudo_potential((float)C.psi_form, C.psi_rho0, C.eos_a, C.eos_b, C.eos_T, C.g_ff, rho);
-        const float old = L.rho_prev[s];
-        rmax = (double)(fabsf(rho - old) / old);
-        L.rho_prev[s] = rho;
+    for (int q = 0; q < 9; q++) drho += df[q];
+    const float rho = C.rho0 + drho;
+    L.psi[s] = pseudo_potential((float)C.psi_form, C.psi_rho0, C.eos_a, C.eos_b, C.eos_T, C.g_ff, rho);
+    const float old = L.rho_prev[s];
+    L.rho_prev[s] = rho;
+    return (double)(fabsf(rho - old) / old);
+}
+
+// pass 1 over the plain cells of the active 32x8 tiles (row masks)
+template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
+{
+    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
+    const uint32_t mask = L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)];
+    const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
+    const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
+    double rmax = 0.0;
+    if ((mask >> (threadIdx.x & 31)) & 1u) rmax = ads_density<P, false>(L, C, o, x, y);
+    if (o.diff) block_max(rmax, C.red + o.red_slot);
+}
+
+// pass 1 over the special cells, from their records (128 per block)
+template <int P> __global__ void __launch_bounds__(128) k_ads_psi_special(LevelView L, Common C, StepOpt o,
+                                                                          int64_t spec_begin, int spec_count)
+{
+    const int i = (int)blockIdx.x * 128 + (int)threadIdx.x;
+    double rmax = 0.0;
+    if (i < spec_count)
+    {
+        const int32_t xy = C.specials[spec_begin + i].xy;
+        rmax = ads_density<P, true>(L, C, o, xy & 0xFFFF, xy >> 16);
     }
     if (o.diff) block_max(rmax, C.red + o.red_slot);
 }
@@ -524,16 +552,24 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, C
 // the same body with the regularized MRT, SRBB walls, no inlet / outlet and the
 // velocity residual (C.collision, C.wall, C.inlet_outlet; o.diff accumulates
 // sum |u| for both terms, as its |u| of the previous step is never stored).
-// psi[r][c]: the pseudopotential at (x + c - 1, y + r - 1)
-template <int P>
+// psi[r][c]: the pseudopotential at (x + c - 1, y + r - 1); SPEC: the cell may
+// be special (its record applies), else it is a plain cell
+template <int P, bool SPEC>
 __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, const StepOpt &o, int x, int y,
                                          const float psi[3][3], double &r_diff, double &r_norm)
 {
     const int64_t s = site_of(L, x, y);
     float df[9];
-    bool special;
+    bool special = false;
     SpecialRec rec;
-    const float omega = load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
+    float omega;
+    if (SPEC) omega = load_cell<P>(L, C, x, y, o.direct, o.first_sub, df, special, rec);
+    else
+    {
+        if (o.direct) load_raw<0>(L, x, y, df);
+        else load_raw<P>(L, x, y, df);
+        omega = L.omega[s];
+    }
     const uint32_t out = special ? ((rec.m1 >> 21) & 0x1FFu) : 0x1FFu;
     const uint32_t wall = special ? ((rec.m0 >> 18) & 0x1FFu) : 0u;
     // sum over the streaming links of w_f psi(x + c) c, formed from psi differences
@@ -600,8 +636,8 @@ __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, co
     store_post<P>(L, x, y, fs);
 }
 
-// The neighbour pseudopotentials come by warp shuffles: a warp holds one row of
-// a 32x8 tile, each lane loads psi of its column in the rows y-1, y, y+1
+// Pass 2 over the plain cells of the active 32x8 tiles.  The neighbour
+// pseudopotentials come by warp shuffles: a warp holds one row of a 32x8 tile, each lane loads psi of its column in the rows y-1, y, y+1
 // (coalesced), and takes the x-neighbours from the adjacent lanes; the lanes at
 // the ends of the row (and the last image column) load their outer neighbours.
 template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
@@ -623,7 +659,30 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, 
         if (inside && (lane == 31 || x + 1 == L.W)) psi[r][2] = L.psi[site_of(L, wrapx(x + 1, L.W), yr)];
     }
     double r_diff = 0.0, r_norm = 0.0;
-    if (inside && L.omega[site_of(L, x, y)] != 0.0f) ads_cell<P>(L, C, o, x, y, psi, r_diff, r_norm);
+    const uint32_t mask = L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)];
+    if ((mask >> lane) & 1u) ads_cell<P, false>(L, C, o, x, y, psi, r_diff, r_norm);
+    if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
+}
+
+// pass 2 over the special cells, from their records; the neighbour
+// pseudopotentials are read directly
+template <int P> __global__ void __launch_bounds__(128) k_ads_step_special(LevelView L, Common C, StepOpt o,
+                                                                           int64_t spec_begin, int spec_count)
+{
+    const int i = (int)blockIdx.x * 128 + (int)threadIdx.x;
+    double r_diff = 0.0, r_norm = 0.0;
+    if (i < spec_count)
+    {
+        const int32_t xy = C.specials[spec_begin + i].xy;
+        const int x = xy & 0xFFFF, y = xy >> 16;
+        float psi[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                psi[r][c] = L.psi[site_of(L, wrapx(x + c - 1, L.W), wrapx(y + r - 1, L.H))];
+        ads_cell<P, true>(L, C, o, x, y, psi, r_diff, r_norm);
+    }
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 

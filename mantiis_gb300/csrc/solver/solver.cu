@@ -205,6 +205,7 @@ struct mgpu_ctx
     DevBuf<double> red;     // kRing * 4
     double *red_host = nullptr; // pinned staging copy of the accumulators
     DevBuf<double> out_rho, out_ux, out_uy, out_f;
+    DevBuf<double> in_rho, in_ux, in_uy; // staging of mgpu_set_equilibrium, kept between calls
     DevBuf<unsigned int> errword;
     float rho0f = 0.f;
     bool adsorption = false; // Shan-Chen step body (include/mantiisApp.hpp:248-265)
@@ -218,6 +219,9 @@ struct mgpu_ctx
 
     cudaGraphExec_t graph = nullptr; // two coarse steps, no residual (throughput path)
     std::string graph_key;           // level parities the graph was captured at
+    cudaGraphExec_t run_graph = nullptr; // two coarse steps with residuals into the scratch slots
+    std::string run_graph_key;
+    int64_t run_graph_launches = 0;
     int64_t graph_launches = 0;
     std::unique_ptr<PhasePlan> plan; // phase engine tables of this image
     std::vector<std::unique_ptr<PhasePlan>> level_plans; // single-level tables (mgpu_step_level)
@@ -478,15 +482,46 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         dev::StepOpt o_psi = o, o_step = o;
         o_psi.diff = (diff && !vel_res) ? 1 : 0;
         o_step.diff = (diff && vel_res) ? 1 : 0;
+        // plain cells over the tiles on the main stream, special cells from their
+        // records on a side stream; pass 2 reads the pseudopotential of every
+        // cell, so both pass-1 kernels finish before either pass-2 kernel
         dim3 grid((unsigned)ll.tile_list.size()), block(256);
+        const int nspec = (int)ll.spec_count;
+        const dim3 sgrid((unsigned)((nspec + 127) / 128));
+        cudaStream_t side = ctx->lanes.special;
+        auto fork = [&]() {
+            CK(cudaEventRecord(ctx->lanes.fork, ctx->stream));
+            CK(cudaStreamWaitEvent(side, ctx->lanes.fork, 0));
+        };
+        auto join = [&]() {
+            CK(cudaEventRecord(ctx->lanes.join_special, side));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->lanes.join_special, 0));
+        };
         if (!ll.tile_list.empty())
         {
+            if (nspec) fork();
             if (o.parity == 0) dev::k_ads_psi<0><<<grid, block, 0, ctx->stream>>>(V, C, o_psi);
             else dev::k_ads_psi<1><<<grid, block, 0, ctx->stream>>>(V, C, o_psi);
             launch_check(ctx);
+            if (nspec)
+            {
+                if (o.parity == 0) dev::k_ads_psi_special<0><<<sgrid, 128, 0, side>>>(V, C, o_psi, ll.spec_begin, nspec);
+                else dev::k_ads_psi_special<1><<<sgrid, 128, 0, side>>>(V, C, o_psi, ll.spec_begin, nspec);
+                launch_check(ctx);
+                join();
+                fork();
+            }
             if (o.parity == 0) dev::k_ads_step<0><<<grid, block, 0, ctx->stream>>>(V, C, o_step);
             else dev::k_ads_step<1><<<grid, block, 0, ctx->stream>>>(V, C, o_step);
             launch_check(ctx);
+            if (nspec)
+            {
+                if (o.parity == 0)
+                    dev::k_ads_step_special<0><<<sgrid, 128, 0, side>>>(V, C, o_step, ll.spec_begin, nspec);
+                else dev::k_ads_step_special<1><<<sgrid, 128, 0, side>>>(V, C, o_step, ll.spec_begin, nspec);
+                launch_check(ctx);
+                join();
+            }
         }
         ctx->lv[0].steps++;
         ctx->coarse_done++;
@@ -626,26 +661,106 @@ void checkpoint_restore(mgpu_ctx *ctx)
 // Steps [k0+1 .. k0+n] with the residual of every step in slots (step index
 // mod kRing).  Kernel of step k reads state k-1, so it evaluates residual k-1;
 // the residual of the last step comes from a read pass.
+// Two coarse steps with residual terms from a CUDA graph (captured once per
+// state of the level parities): the graph zeroes the two scratch slots past the
+// ring, both steps accumulate into them, and they are then copied to ring slots
+// `first` and `first + 1` (mod kRing).  Launch overhead, not GPU work, limits
+// small images stepped one call at a time; the graph takes it off the host.
+void run_pair_graph(mgpu_ctx *ctx, bool store_u, int first)
+{
+    const std::string key = state_key({ctx}, 0) + (ctx->adsorption ? "a" : "t");
+    if (ctx->run_graph && ctx->run_graph_key != key)
+    {
+        CK(cudaGraphExecDestroy(ctx->run_graph));
+        ctx->run_graph = nullptr;
+    }
+    double *scratch = ctx->red.p + (size_t)kRing * 4;
+    if (!ctx->run_graph)
+    {
+        if (ctx->plan)
+        {
+            plan_variant(*ctx->plan, {ctx}, 0);
+            plan_variant(*ctx->plan, {ctx}, 1);
+        }
+        std::vector<int64_t> saved;
+        for (auto &l : ctx->lv) saved.push_back(l.steps);
+        const int64_t saved_done = ctx->coarse_done, saved_launch = ctx->launches;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        CK(cudaMemsetAsync(scratch, 0, 8 * sizeof(double), ctx->stream));
+        coarse_step(ctx, true, store_u, kRing * 4);
+        coarse_step(ctx, true, store_u, (kRing + 1) * 4);
+        CK(cudaStreamEndCapture(ctx->stream, &g));
+        CK(cudaGraphInstantiate(&ctx->run_graph, g, 0));
+        CK(cudaGraphDestroy(g));
+        ctx->run_graph_key = key;
+        ctx->run_graph_launches = ctx->launches - saved_launch;
+        for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
+        ctx->coarse_done = saved_done;
+        ctx->launches = saved_launch;
+    }
+    CK(cudaGraphLaunch(ctx->run_graph, ctx->stream));
+    for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps += 2 * ctx->lay.levels[l].substeps;
+    ctx->coarse_done += 2;
+    ctx->launches += ctx->run_graph_launches;
+    first %= kRing;
+    const int a = first + 1 < kRing ? 2 : 1;
+    CK(cudaMemcpyAsync(ctx->red.p + (size_t)first * 4, scratch, (size_t)a * 4 * sizeof(double),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    if (a == 1)
+        CK(cudaMemcpyAsync(ctx->red.p, scratch + 4, 4 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+}
+
+bool fresh_state(const mgpu_ctx *ctx)
+{
+    for (auto &l : ctx->lv)
+        if (l.steps == 0) return true;
+    return false;
+}
+
+// Steps [k0+1 .. k0+n] with the residual of every step in slots (step index
+// mod kRing).  Kernel of step k reads state k-1, so it evaluates residual k-1;
+// the residual of the last step comes from a read pass.  Pairs of steps run
+// from a CUDA graph (not for coupled runs, whose phase switch is host-side,
+// nor from the initial "direct" state).
 void run_batch_with_residuals(mgpu_ctx *ctx, int n)
 {
     int64_t k0 = ctx->coarse_done;
     zero_slots(ctx, (int)((k0 + 1) % kRing), n);
+    const bool graphs = !ctx->coupled;
     if (ctx->adsorption)
     {
         // the density change of step k is known within step k
-        for (int i = 0; i < n; i++)
+        for (int i = 0; i < n;)
         {
             int64_t k = ctx->coarse_done + 1;
-            coarse_step(ctx, true, false, (int)((k % kRing) * 4));
+            if (graphs && n - i >= 2 && !fresh_state(ctx))
+            {
+                run_pair_graph(ctx, false, (int)(k % kRing));
+                i += 2;
+            }
+            else
+            {
+                coarse_step(ctx, true, false, (int)((k % kRing) * 4));
+                i++;
+            }
         }
         return;
     }
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < n;)
     {
         int64_t k = ctx->coarse_done + 1; // this step
         bool diff = i > 0;                // residual of step k-1 (the previous batch closed its own last one)
-        int slot = (int)(((k - 1) % kRing) * 4);
-        coarse_step(ctx, diff, true, slot);
+        if (diff && graphs && n - i >= 2 && !fresh_state(ctx))
+        {
+            run_pair_graph(ctx, true, (int)((k - 1) % kRing));
+            i += 2;
+        }
+        else
+        {
+            coarse_step(ctx, diff, true, (int)(((k - 1) % kRing) * 4));
+            i++;
+        }
     }
     int64_t last = ctx->coarse_done;
     cells_pass(ctx, nullptr, nullptr, nullptr, nullptr, true, false, (int)((last % kRing) * 4));
@@ -1135,7 +1250,7 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     ctx->ibuf.zero(s);
     ctx->cell_level.upload(ctx->lay.cell_level, acct, s);
     ctx->cell_site.upload(ctx->lay.cell_site, acct, s);
-    ctx->red.alloc((size_t)kRing * 4, acct);
+    ctx->red.alloc((size_t)(kRing + 2) * 4, acct); // the ring and two scratch slots
     ctx->red.zero(s);
     ctx->errword.alloc(1, acct);
     ctx->errword.zero(s);
@@ -1205,6 +1320,7 @@ int mgpu_destroy(mgpu_ctx *ctx)
     if (!ctx) return MGPU_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
     ctx->lanes.destroy();
     if (ctx->red_host) cudaFreeHost(ctx->red_host);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1559,14 +1675,25 @@ int mgpu_set_equilibrium(mgpu_ctx *ctx, const double *rho, const double *ux, con
 {
     return guarded(ctx, [&]() {
         if (!ctx || !rho || !ux || !uy) throw std::invalid_argument("null argument");
-        int64_t n = ctx->grid.n_cells, tmp = 0;
-        DevBuf<double> dr, du, dv;
-        dr.upload(std::vector<double>(rho, rho + n), tmp, ctx->stream);
-        du.upload(std::vector<double>(ux, ux + n), tmp, ctx->stream);
-        dv.upload(std::vector<double>(uy, uy + n), tmp, ctx->stream);
+        const int64_t n = ctx->grid.n_cells;
+        if (n == 0) return MGPU_OK;
+        if (ctx->in_rho.n < (size_t)n)
+        {
+            int64_t acct = 0;
+            ctx->in_rho.alloc(n, acct);
+            ctx->in_ux.alloc(n, acct);
+            ctx->in_uy.alloc(n, acct);
+            ctx->bytes += acct;
+        }
+        // straight from the caller's buffers (fast when they are pinned); the
+        // call returns after the copies, so the buffers are free again
+        CK(cudaMemcpyAsync(ctx->in_rho.p, rho, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->in_ux.p, ux, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->in_uy.p, uy, n * 8, cudaMemcpyHostToDevice, ctx->stream));
         for (auto &l : ctx->lv) l.steps = 0;
         dev::k_set_equilibrium<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
-            ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, dr.p, du.p, dv.p);
+            ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, ctx->in_rho.p, ctx->in_ux.p,
+            ctx->in_uy.p);
         launch_check(ctx);
         CK(cudaStreamSynchronize(ctx->stream));
         return MGPU_OK;

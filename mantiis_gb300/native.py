@@ -331,9 +331,19 @@ class Solver:
         lib().mgpu_residuals(self._h, _ptr(out), cnt.value, C.byref(cnt))
         return out
 
-    def cells(self, with_f=False):
+    def cells(self, with_f=False, out=None):
+        """FP64 fields per cell (mgpu_download_cells); `out` may hold float64
+        arrays rho, ux, uy of n_cells each (e.g. views of pinned host memory) to
+        read into."""
         N = self.n_cells
-        rho, ux, uy = np.zeros(N), np.zeros(N), np.zeros(N)
+        if out is not None:
+            rho, ux, uy = (np.ascontiguousarray(out[k]) for k in ("rho", "ux", "uy"))
+            if not all(a.dtype == np.float64 and a.size == N for a in (rho, ux, uy)):
+                raise ValueError("out arrays must be float64 of n_cells each")
+            if any(a is not out[k] for a, k in zip((rho, ux, uy), ("rho", "ux", "uy"))):
+                raise ValueError("out arrays must be contiguous")
+        else:
+            rho, ux, uy = np.zeros(N), np.zeros(N), np.zeros(N)
         f = np.zeros(9 * N) if with_f else None
         self._check(lib().mgpu_download_cells(self._h, _ptr(rho), _ptr(ux), _ptr(uy), _ptr(f)))
         out = dict(rho=rho, ux=ux, uy=uy)
