@@ -108,6 +108,8 @@ class ClockSampler:
 WORKLOADS = {
     "config2": WORKLOAD,
     "single1024": "1024x1024 seeded disk images (r U[6,40], porosity 0.6), single block, Kn 0.1",
+    "config4": "config4: seeded disk images of side {128..2048}, porosity U[0.45,0.75], 1-3 levels, "
+               "log-uniform Kn in [0.01, 2], stepped together (uneven sizes and depths)",
 }
 
 
@@ -116,6 +118,8 @@ def make_images(count, offset, workload="config2"):
 
     if workload == "single1024":
         return [dict(workloads.image(1024, 6, 40, 0.6, 0.1, 5000 + offset + i), levels=1) for i in range(count)]
+    if workload == "config4":
+        return [workloads.config4(offset + i) for i in range(count)]
     return [dict(workloads.config2(offset + i), levels=3) for i in range(count)]
 
 
@@ -446,8 +450,9 @@ def main():
             "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": warm,
             "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "images_per_gpu": len(imgs), "n": 1024,
-                       "levels": imgs[0]["levels"],
+            "config": {"workload": WORKLOADS[args.workload], "images_per_gpu": len(imgs),
+                       "n": [int(im["pore"].shape[0]) for im in imgs] if args.workload == "config4" else 1024,
+                       "levels": [int(im["levels"]) for im in imgs] if args.workload == "config4" else imgs[0]["levels"],
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
                        "l2": "inputs larger than L2 (state of the batch > 129 MB)",
                        "graph": "one CUDA graph of 2 coarse steps for the whole batch, each image on its own stream",
