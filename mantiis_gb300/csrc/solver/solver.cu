@@ -1424,11 +1424,21 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
         auto flush = [&]() {
             if (pending.empty()) return;
             std::vector<double> v(pending.size() * 4);
-            for (size_t i = 0; i < pending.size(); i++) read_slot(ctx, (int)pending[i], &v[i * 4]);
-            CK(cudaStreamSynchronize(ctx->stream));
+            // consecutive slots in one read
+            size_t a = 0;
+            while (a < pending.size())
+            {
+                size_t b = a + 1;
+                while (b < pending.size() && pending[b] == pending[b - 1] + 1 && (int)(b - a) < kRing) b++;
+                read_slots(ctx, (int)(pending[a] % kRing), (int)(b - a), &v[a * 4]);
+                a = b;
+            }
             for (size_t i = 0; i < pending.size(); i++) ctx->residuals.push_back(residual_of(ctx, &v[i * 4]));
             pending.clear();
         };
+        // with a residual every step, pairs of steps replay a CUDA graph (not for
+        // coupled runs, whose phase switch is host-side, nor from the initial state)
+        auto pairs_ok = [&](int i) { return K == 1 && !ctx->coupled && n_steps - i >= 2 && !fresh_state(ctx); };
         for (int i = 0; i < n_steps; i++)
         {
             int64_t k = ctx->coarse_done + 1;
@@ -1439,20 +1449,40 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
             }
             if (ctx->adsorption)
             {
-                bool diff = (k % K == 0);
-                if (diff) zero_slots(ctx, (int)(k % kRing), 1);
-                coarse_step(ctx, diff, false, (int)((k % kRing) * 4));
-                if (diff) pending.push_back(k);
+                if (pairs_ok(i))
+                {
+                    run_pair_graph(ctx, false, (int)(k % kRing));
+                    pending.push_back(k);
+                    pending.push_back(k + 1);
+                    i++;
+                }
+                else
+                {
+                    bool diff = (k % K == 0);
+                    if (diff) zero_slots(ctx, (int)(k % kRing), 1);
+                    coarse_step(ctx, diff, false, (int)((k % kRing) * 4));
+                    if (diff) pending.push_back(k);
+                }
                 if ((int)pending.size() >= kRing / 2) flush();
                 continue;
             }
             // residual of step s is evaluated by kernel s+1 against |u| stored by kernel s
             bool diff = k >= 2 && ((k - 1) % K == 0);
             bool store = (k % K == 0);
-            int slot = (int)(((k - 1) % kRing) * 4);
-            if (diff) zero_slots(ctx, (int)((k - 1) % kRing), 1);
-            coarse_step(ctx, diff, store, slot);
-            if (diff) pending.push_back(k - 1);
+            if (diff && pairs_ok(i))
+            {
+                run_pair_graph(ctx, true, (int)((k - 1) % kRing));
+                pending.push_back(k - 1);
+                pending.push_back(k);
+                i++;
+            }
+            else
+            {
+                int slot = (int)(((k - 1) % kRing) * 4);
+                if (diff) zero_slots(ctx, (int)((k - 1) % kRing), 1);
+                coarse_step(ctx, diff, store, slot);
+                if (diff) pending.push_back(k - 1);
+            }
             if ((int)pending.size() >= kRing / 2) flush();
         }
         flush();

@@ -212,3 +212,22 @@ def test_plain_paths_agree_and_autotune():
     assert min(us) > 0
     assert runs[-1][1]["plain_path"] == int(np.argmin(us))
     record("autotune_256", direct_us=us[0], tma_us=us[1], direct8x4_us=us[2])
+
+
+@pytest.mark.parametrize("sim", ["transport", "adsorption"])
+def test_advance_residuals_equal_run(fixture64, sim):
+    # mgpu_advance with a residual every step (pairs of steps from a CUDA graph)
+    # records the residuals mgpu_run records (FP64 atomic sums: 1e-12)
+    from mantiis_gb300 import SIM_ADSORPTION
+
+    kw = dict(dx=12e-9, simulation=SIM_ADSORPTION) if sim == "adsorption" else dict(dx=1e-9)
+    a = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(tol=0.0, **kw))
+    b = Solver(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(tol=0.0, check_every=1, **kw))
+    assert a.run(31) == 31
+    b.advance(31)
+    b.sync()
+    ra, rb = a.residuals(), b.residuals()
+    n = min(len(ra), len(rb))
+    assert n >= 30
+    assert np.allclose(ra[:n], rb[:n], rtol=1e-12, atol=0)
+    assert np.array_equal(a.cells(with_f=True)["f"], b.cells(with_f=True)["f"])
