@@ -1894,8 +1894,9 @@ struct mgpu_batch
     SideLanes lanes;
     bool own_stream = false;
     cudaEvent_t ev_done = nullptr;
-    // images step concurrently, each on its own stream (with its own side
-    // lanes), forked from and joined back to `stream` around their coarse steps
+    // images step on a few concurrent streams (each with its own side lanes),
+    // image i on stream i % streams, forked from and joined back to `stream`
+    // around their coarse steps
     std::vector<cudaStream_t> img_stream;
     std::vector<SideLanes> img_lanes;
     std::vector<cudaEvent_t> img_done;
@@ -1939,13 +1940,16 @@ void batch_step(mgpu_batch *b, int n = 1)
     else
     {
         CK(cudaEventRecord(b->ev_start, b->stream));
+        const size_t ns = b->img_stream.size();
+        for (size_t j = 0; j < ns; j++) CK(cudaStreamWaitEvent(b->img_stream[j], b->ev_start, 0));
         for (size_t i = 0; i < b->ctxs.size(); i++)
-        {
-            CK(cudaStreamWaitEvent(b->img_stream[i], b->ev_start, 0));
             for (int k = 0; k < n; k++)
-                phase_step(*b->ctxs[i]->plan, {b->ctxs[i]}, b->img_stream[i], b->img_lanes[i], none, b->launches);
-            CK(cudaEventRecord(b->img_done[i], b->img_stream[i]));
-            CK(cudaStreamWaitEvent(b->stream, b->img_done[i], 0));
+                phase_step(*b->ctxs[i]->plan, {b->ctxs[i]}, b->img_stream[i % ns], b->img_lanes[i % ns], none,
+                           b->launches);
+        for (size_t j = 0; j < ns; j++)
+        {
+            CK(cudaEventRecord(b->img_done[j], b->img_stream[j]));
+            CK(cudaStreamWaitEvent(b->stream, b->img_done[j], 0));
         }
     }
     for (auto *c : b->ctxs) c->ref_t += n;
@@ -1976,13 +1980,24 @@ int mgpu_batch_create(mgpu_ctx *const *ctxs, int n, mgpu_batch **out)
         b->own_stream = true;
         b->lanes.create();
         CK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
+        // concurrent streams: as many images as fit twice the L2 together (at
+        // least 2: one image's small launches then overlap another's work; more
+        // large images at once evict each other's levels from L2 -- config-2
+        // images, ~110 MB each: 2 streams 13.4 k MLUPS, 4 or 8 streams 12.2 k)
+        int l2 = 0;
+        CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+        int64_t bytes = 0;
+        for (auto *c : b->ctxs) bytes += c->bytes;
+        const double per = (double)bytes / (double)b->ctxs.size();
+        const int streams = (int)std::max<double>(2.0, std::min<double>((double)b->ctxs.size(),
+                                                                        std::floor(2.0 * l2 / std::max(per, 1.0))));
         if (b->ctxs.size() > 1)
         {
             CK(cudaEventCreateWithFlags(&b->ev_start, cudaEventDisableTiming));
-            b->img_stream.resize(b->ctxs.size());
-            b->img_lanes.resize(b->ctxs.size());
-            b->img_done.resize(b->ctxs.size());
-            for (size_t i = 0; i < b->ctxs.size(); i++)
+            b->img_stream.resize((size_t)streams);
+            b->img_lanes.resize((size_t)streams);
+            b->img_done.resize((size_t)streams);
+            for (int i = 0; i < streams; i++)
             {
                 CK(cudaStreamCreateWithFlags(&b->img_stream[i], cudaStreamNonBlocking));
                 b->img_lanes[i].create();
