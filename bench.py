@@ -455,7 +455,7 @@ def main():
                        "levels": [int(im["levels"]) for im in imgs] if args.workload == "config4" else imgs[0]["levels"],
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
                        "l2": "inputs larger than L2 (state of the batch > 129 MB)",
-                       "graph": "one CUDA graph of 2 coarse steps for the whole batch, each image on its own stream",
+                       "graph": "one CUDA graph of 2 coarse steps for the whole batch, images on L2-sized concurrent streams",
                        "state_finite_after_timed_steps": finite},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
