@@ -40,6 +40,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 BYTES_PER_LU = 72.0
+# host threads of the end-to-end leg, each stepping its share of the images in
+# turn: two large images in flight at once share the L2 best (config 2, 1 / 2 / 4
+# threads: 9.2 / 8.9 / 8.4 k MLUPS; single-block 1024^2: 13.7 / 16.9 / 12.0 k)
+E2E_THREADS = 2
 WORKLOAD = "config2: 1024x1024 seeded disk images (r U[6,40], porosity U[0.5,0.7]), 3-level quadtree, Kn U[0.01,1]"
 
 
@@ -395,8 +399,9 @@ def main():
             traffic = None
     prof.close()
 
-    # end to end through the public API with host buffers: every image on its
-    # own host thread and stream (contexts are independent and single-threaded);
+    # end to end through the public API with host buffers: the images on
+    # E2E_THREADS host threads, each context on its own stream (contexts are
+    # independent and single-threaded);
     # per image the equilibrium state is uploaded, Ke steps run with the per-step
     # residual and break test, and the cell fields are read back
     Ke = args.e2e_steps
@@ -425,7 +430,7 @@ def main():
 
     from concurrent.futures import ThreadPoolExecutor
 
-    with ThreadPoolExecutor(len(solvers)) as ex:
+    with ThreadPoolExecutor(min(len(solvers), E2E_THREADS)) as ex:
         # untimed: plans, checkpoint buffers and the two-step residual graph
         list(ex.map(lambda i: e2e_image(i, 5), range(len(solvers))))
         torch.cuda.synchronize()
