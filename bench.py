@@ -7,11 +7,11 @@ A bench step is one coarse time step of every image of the batch.
 
   value     MLUPS over the batch, device-timed with CUDA events around K steps
             replayed from CUDA graphs (state resident in HBM)
-  e2e       MLUPS through the public C ABI with host buffers: per image, on its
-            own host thread and stream, the equilibrium state is uploaded
-            (mgpu_set_equilibrium), K steps run with the reference's per-step
-            residual and break test (mgpu_run), and the per-cell fields are read
-            back (mgpu_download_cells)
+  e2e       MLUPS through the public C ABI with pinned host buffers: per image
+            (two host threads, each context on its own stream) the equilibrium
+            state is uploaded (mgpu_set_equilibrium), K steps run with the
+            reference's per-step residual and break test (mgpu_run), and the
+            per-cell fields are read back (mgpu_download_cells)
   roofline  the finest-level step kernel: 72 B per lattice update (9 FP32
             populations read + 9 written) over its CUDA-event launch time
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference's step)
