@@ -220,8 +220,9 @@ int64_t mgpu_launch_count(const mgpu_ctx *ctx);
 /* ---- batched stepping (no reference counterpart: the reference runs one
  * image per process, include/mantiisApp.hpp:286-430) ----
  * A batch steps a group of transport contexts of the current device together:
- * each phase of a coarse step is one launch over every image, each interface
- * wave one launch, two coarse steps are replayed from one CUDA graph.  The
+ * two coarse steps of every image are replayed from one CUDA graph in which the
+ * images run on a few concurrent streams (as many as fit twice the L2 cache,
+ * at least 2), so one image's small launches overlap another's work.  The
  * contexts keep their state and stay usable on their own; batch work is
  * ordered after earlier work on each context's stream and before later work.
  * A context must not be stepped by two batches at once. */
