@@ -231,3 +231,27 @@ def test_advance_residuals_equal_run(fixture64, sim):
     assert n >= 30
     assert np.allclose(ra[:n], rb[:n], rtol=1e-12, atol=0)
     assert np.array_equal(a.cells(with_f=True)["f"], b.cells(with_f=True)["f"])
+
+
+def test_config2_full_size_vs_oracle():
+    # the benchmark's own workload at full size: a 1024x1024 config-2 image, 3
+    # levels, edge_fine, 6 coarse steps on the GPU against the FP64 oracle
+    # (all host cores); populations relative to rho_in, u_x relative to its max
+    import os
+    from mantiis_gb300 import workloads
+
+    img = workloads.config2(0)
+    p = default_params(multiblock=1, max_allowed_level=3, dx=img["dx"], edge_fine=1)
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
+    o = for_grid(g, sim="transport", dx=img["dx"], threads=os.cpu_count() or 1)
+    o.run(6)
+    ref = o.fields()
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    assert s.info["max_level"] == 3
+    s.advance(6)
+    got = s.cells(with_f=True)
+    rho_in = s.info["rho_in"]
+    e_f = np.abs(got["f"].reshape(-1) - np.asarray(ref["f"]).reshape(-1)).max() / rho_in
+    e_ux = rel_err(got["ux"], ref["ux"])
+    record("config2_1024_vs_oracle_6", f=e_f, ux=e_ux)
+    assert e_f < 1e-6 and e_ux < 1e-4
