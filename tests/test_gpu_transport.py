@@ -255,3 +255,27 @@ def test_config2_full_size_vs_oracle():
     e_ux = rel_err(got["ux"], ref["ux"])
     record("config2_1024_vs_oracle_6", f=e_f, ux=e_ux)
     assert e_f < 1e-6 and e_ux < 1e-4
+
+
+def test_config1_permeability_vs_oracle():
+    # config 1 (128x128 seeded disks, radii U[4,10], porosity 0.65, Kn ~0.1,
+    # single block) for its Nt = 5000 steps: the permeability k = <u_x> nu / F
+    # of the GPU run within 1e-5 of the FP64 oracle's
+    import os
+    from mantiis_gb300 import workloads
+
+    img = workloads.config1(0)
+    p = default_params(dx=img["dx"], tol=0.0)
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
+    o = for_grid(g, sim="transport", dx=img["dx"], fbody=p.fbody, threads=os.cpu_count() or 1)
+    o.run(5000)
+    ref = o.fields()
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    s.advance(5000)
+    k_gpu = s.observables()["permeability"]
+    n = img["pore"].shape[0]
+    nu = (s.info["tau_mean"] - 0.5) / 3.0
+    k_ref = ref["ux"].sum() / (n * n) * nu / p.fbody
+    e = abs(k_gpu - k_ref) / abs(k_ref)
+    record("config1_permeability_5000", rel=e, k=k_gpu)
+    assert e < 1e-5
