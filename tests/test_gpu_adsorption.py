@@ -93,3 +93,32 @@ def test_coupled_run_matches_reference_code(fixture64):
         assert e_f < 1e-5 and e_ux < 1e-3 and e_rho < 1e-4
     r = s.residuals()
     assert len(r) == 130 and np.allclose(r[100:], 1.0)
+
+
+def test_config3_full_size_vs_oracle():
+    # config 3 at full size: 512x512 seeded disk image, porosity 0.6,
+    # psi = rho0 (1 - exp(-rho/rho0)), G = -4.5, G_ads = -0.5 (common
+    # convention; G_ff = G / 18, G_fs = 3 G_ads in the reference's), initial
+    # density 0.5 +- 1e-3, 200 steps: the density field (adsorbed layers) and the
+    # total mass against the FP64 oracle
+    import os
+    from mantiis_gb300 import workloads
+
+    img = workloads.config3(0)
+    kw = dict(psi_form=1, rho_psi=0.5, g_ff=-4.5 / 18, g_fs=-1.5)
+    p = default_params(dx=img["dx"], simulation=SIM_ADSORPTION, rho_init=0.5, fbody=0.0, tol=0.0, **kw)
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
+    rng = np.random.default_rng(3000)
+    rho = 0.5 + rng.uniform(-1e-3, 1e-3, g.n_cells)
+    o = for_grid(g, sim="adsorption", dx=img["dx"], fbody=0.0, rho_init=rho, threads=os.cpu_count() or 1, **kw)
+    o.run(200)
+    ref = o.fields()
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    s.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
+    s.run(200)
+    got = s.cells()
+    e_rho = np.abs(got["rho"] - ref["rho"]).max() / np.abs(ref["rho"]).max()
+    m_gpu, m_ref, m0 = got["rho"].sum(), ref["rho"].sum(), rho.sum()
+    record("config3_512_200", rho=e_rho, mass=abs(m_gpu - m_ref) / m_ref, drift_ref=abs(m_ref - m0) / m0,
+           rho_span=float(ref["rho"].max() - ref["rho"].min()))
+    assert e_rho < 1e-5 and abs(m_gpu - m_ref) / m_ref < 1e-6
