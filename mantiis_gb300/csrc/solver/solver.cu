@@ -183,6 +183,36 @@ struct SideLanes
     }
 };
 
+// Captures the work enqueued on `st` between construction and take() into a
+// graph; if an exception leaves the scope first, the capture is ended and its
+// partial graph dropped, so the stream is usable again.
+struct StreamCapture
+{
+    cudaStream_t st;
+    bool open = false;
+    explicit StreamCapture(cudaStream_t s) : st(s)
+    {
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        open = true;
+    }
+    cudaGraph_t take()
+    {
+        cudaGraph_t g = nullptr;
+        open = false;
+        CK(cudaStreamEndCapture(st, &g));
+        return g;
+    }
+    ~StreamCapture()
+    {
+        if (!open) return;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+        cudaGetLastError();
+    }
+    StreamCapture(const StreamCapture &) = delete;
+    StreamCapture &operator=(const StreamCapture &) = delete;
+};
+
 struct mgpu_ctx
 {
     mgpu_params prm{};
@@ -685,19 +715,35 @@ void run_pair_graph(mgpu_ctx *ctx, bool store_u, int first)
         std::vector<int64_t> saved;
         for (auto &l : ctx->lv) saved.push_back(l.steps);
         const int64_t saved_done = ctx->coarse_done, saved_launch = ctx->launches;
+        // capturing advances the host-side step counters; put them back either way
+        auto restore = [&]() {
+            for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
+            ctx->coarse_done = saved_done;
+            ctx->launches = saved_launch;
+        };
         cudaGraph_t g;
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        CK(cudaMemsetAsync(scratch, 0, 8 * sizeof(double), ctx->stream));
-        coarse_step(ctx, true, store_u, kRing * 4);
-        coarse_step(ctx, true, store_u, (kRing + 1) * 4);
-        CK(cudaStreamEndCapture(ctx->stream, &g));
-        CK(cudaGraphInstantiate(&ctx->run_graph, g, 0));
-        CK(cudaGraphDestroy(g));
+        try
+        {
+            StreamCapture cap(ctx->stream);
+            CK(cudaMemsetAsync(scratch, 0, 8 * sizeof(double), ctx->stream));
+            coarse_step(ctx, true, store_u, kRing * 4);
+            coarse_step(ctx, true, store_u, (kRing + 1) * 4);
+            g = cap.take();
+        }
+        catch (...)
+        {
+            restore();
+            throw;
+        }
+        const int64_t captured = ctx->launches - saved_launch;
+        restore();
+        {
+            const cudaError_t e_inst = cudaGraphInstantiate(&ctx->run_graph, g, 0);
+            cudaGraphDestroy(g);
+            CK(e_inst);
+        }
         ctx->run_graph_key = key;
-        ctx->run_graph_launches = ctx->launches - saved_launch;
-        for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
-        ctx->coarse_done = saved_done;
-        ctx->launches = saved_launch;
+        ctx->run_graph_launches = captured;
     }
     CK(cudaGraphLaunch(ctx->run_graph, ctx->stream));
     for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps += 2 * ctx->lay.levels[l].substeps;
@@ -1523,17 +1569,31 @@ int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
             std::vector<int64_t> saved;
             for (auto &l : ctx->lv) saved.push_back(l.steps);
             int64_t saved_done = ctx->coarse_done, saved_launch = ctx->launches;
+            auto restore = [&]() {
+                for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
+                ctx->coarse_done = saved_done;
+                ctx->launches = saved_launch;
+            };
             cudaGraph_t g;
-            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            coarse_step(ctx, false, false, 0);
-            coarse_step(ctx, false, false, 0);
-            CK(cudaStreamEndCapture(ctx->stream, &g));
-            CK(cudaGraphInstantiate(&ctx->graph, g, 0));
-            CK(cudaGraphDestroy(g));
+            try
+            {
+                StreamCapture cap(ctx->stream);
+                coarse_step(ctx, false, false, 0);
+                coarse_step(ctx, false, false, 0);
+                g = cap.take();
+            }
+            catch (...)
+            {
+                restore();
+                throw;
+            }
             ctx->graph_launches = ctx->launches - saved_launch;
-            for (size_t l = 0; l < ctx->lv.size(); l++) ctx->lv[l].steps = saved[l];
-            ctx->coarse_done = saved_done;
-            ctx->launches = saved_launch;
+            restore();
+            {
+                const cudaError_t e_inst = cudaGraphInstantiate(&ctx->graph, g, 0);
+                cudaGraphDestroy(g);
+                CK(e_inst);
+            }
         }
         while (left >= 2)
         {
@@ -2052,19 +2112,35 @@ int mgpu_batch_advance(mgpu_batch *b, int n_steps)
                 saved_t.push_back(c->ref_t);
             }
             const int64_t l0 = b->launches;
+            // capturing advances the host-side step counters; put them back either way
+            auto restore = [&]() {
+                b->launches = l0;
+                for (size_t i = 0; i < b->ctxs.size(); i++)
+                {
+                    for (size_t l = 0; l < b->ctxs[i]->lv.size(); l++) b->ctxs[i]->lv[l].steps = saved[i][l];
+                    b->ctxs[i]->coarse_done = saved_done[i];
+                    b->ctxs[i]->ref_t = saved_t[i];
+                }
+            };
             cudaGraph_t g;
-            CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            batch_step(b, 2);
-            CK(cudaStreamEndCapture(b->stream, &g));
-            CK(cudaGraphInstantiate(&b->graph, g, 0));
-            CK(cudaGraphDestroy(g));
-            b->graph_launches = b->launches - l0;
-            b->launches = l0;
-            for (size_t i = 0; i < b->ctxs.size(); i++)
+            try
             {
-                for (size_t l = 0; l < b->ctxs[i]->lv.size(); l++) b->ctxs[i]->lv[l].steps = saved[i][l];
-                b->ctxs[i]->coarse_done = saved_done[i];
-                b->ctxs[i]->ref_t = saved_t[i];
+                StreamCapture cap(b->stream);
+                batch_step(b, 2);
+                g = cap.take();
+            }
+            catch (...)
+            {
+                restore();
+                b->graph_key.clear();
+                throw;
+            }
+            b->graph_launches = b->launches - l0;
+            restore();
+            {
+                const cudaError_t e_inst = cudaGraphInstantiate(&b->graph, g, 0);
+                cudaGraphDestroy(g);
+                CK(e_inst);
             }
         }
         while (left >= 2)
