@@ -273,14 +273,19 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         L.specials.push_back(rec);
         spec_level.push_back(l);
     }
-    // special records grouped by level and ordered by 8x4 block of sites (row-major
-    // blocks, row-major inside a block), so a warp of the special-cell kernel
-    // covers a compact patch and its neighbour reads share sectors
+    // special records grouped by level, then by whether they have wall links,
+    // then ordered by 8x4 block of sites (row-major blocks, row-major inside a
+    // block), so a warp of the special-cell kernel takes one path over a
+    // compact patch
     {
         std::vector<int64_t> order(L.specials.size());
         for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
         std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
             if (spec_level[a] != spec_level[b]) return spec_level[a] < spec_level[b];
+            // cells with wall links (the longer path) apart from the others, so
+            // the warps of the special-cell kernel take one path
+            const bool wa = ((L.specials[a].m0 >> 18) & 0x1FFu) != 0, wb = ((L.specials[b].m0 >> 18) & 0x1FFu) != 0;
+            if (wa != wb) return wa < wb;
             return special_order_key(L.specials[a].xy) < special_order_key(L.specials[b].xy);
         });
         std::vector<SpecialRec> sorted(order.size());
