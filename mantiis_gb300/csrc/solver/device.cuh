@@ -39,8 +39,9 @@ struct LevelView
     float *rho_prev;      // per site density at the start of the previous step (adsorption), may be null
     const int32_t *tiles; // active 32x8 tiles
     const uint32_t *tile_mask; // 8 row masks of plain cells per active tile
-    const int32_t *tiles8;     // 8x4 tiles holding a plain cell
-    const uint32_t *tile8_mask;// their plain cells (bit = 8 * row + column)
+    const int32_t *tiles8;     // 8x4 tiles holding a plain or light cell
+    const uint32_t *tile8_mask;// their plain and light cells (bit = 8 * row + column)
+    const uint32_t *tile8_light;// their light cells (special only by missing arrivals / buffer status)
     int ntiles, tiles_x;
     int ntiles8;
     int W, H, pitch;

@@ -206,7 +206,11 @@ __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, 
 // Plain cells of one 8x4 tile, one warp per tile (lane = 8 * row + column):
 // the same cell update as plain_tile; on sparse levels these tiles hold a
 // larger share of active cells than 32x8 tiles, so fewer lanes idle and fewer
-// sectors are fetched for inactive sites.
+// sectors are fetched for inactive sites.  The tile's light cells (special only
+// through missing arrivals and buffer status: most of the interface ring of a
+// finer level) are stepped here too, with the reads of special_cell for such a
+// record (interpolated values at the first substep, else the arrivals plus the
+// constant row), so the special-cell kernel keeps only the cells with walls.
 template <int P>
 __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C, const StepOpt &o, int t, int diff,
                                             int store_u, double &r_diff, double &r_norm)
@@ -215,14 +219,47 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
     const int tile = __ldg(&L.tiles8[t]); // tx | ty << 16, in 8- and 4-site units
     const uint32_t mask = __ldg(&L.tile8_mask[t]);
     if (!((mask >> lane) & 1u)) return;
+    const bool light = (__ldg(&L.tile8_light[t]) >> lane) & 1u;
     const int tx = tile & 0xFFFF, ty = tile >> 16;
     const int x = tx * 8 + (lane & 7), y = ty * 4 + (lane >> 3);
     // tiles off the border reach their neighbours without wrapping
     const bool interior = tx > 0 && tx + 1 < (L.W + 7) / 8 && ty > 0 && ty + 1 < (L.H + 3) / 4;
     const int64_t s = site_of(L, x, y);
     float df[9];
-    load_raw_ro<P>(L, x, y, df, interior);
-    const float om = __ldg(&L.omega[s]);
+    float om;
+    if (!light)
+    {
+        load_raw_ro<P>(L, x, y, df, interior);
+        om = __ldg(&L.omega[s]);
+    }
+    else
+    {
+        const SpecialRec rec = C.specials[__ldg(&L.spec[s])];
+        const uint32_t arrive = rec.m0 & 0x1FFu, flags = (rec.m1 >> 17) & 0xFu;
+        om = rec.omega;
+        if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
+        {
+#pragma unroll
+            for (int q = 0; q < 9; q++) df[q] = C.ibuf[(size_t)q * C.n_buf + rec.buf];
+        }
+        else
+        {
+            // a direct state has parity 0: own slots, as load_raw<0>
+            load_raw_ro<P>(L, x, y, df, interior);
+            if (!o.direct)
+            {
+                const bool has_k = (flags & SF_HAS_K) != 0;
+                const float *k = C.ktab + (size_t)(has_k ? rec.k_row : 0) * 9;
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                {
+                    float v = ((arrive >> q) & 1u) ? df[q] : 0.0f;
+                    if (has_k) v += __ldg(&k[q]);
+                    df[q] = v;
+                }
+            }
+        }
+    }
     SpecialRec none;
     step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior);
 }

@@ -14,6 +14,16 @@ namespace
 {
 // ordering key of a special record's site (x | y << 16): 8x4 blocks in row-major
 // order, then row-major inside the block
+// a special record is light when only missing arrivals (with their constant
+// row) and buffer status make it special: no wall link, no x-periodic override,
+// no quirk link, no inlet / outlet role
+inline bool special_is_light(const SpecialRec &r)
+{
+    const uint32_t over = (r.m0 >> 9) & 0x1FFu, wall = (r.m0 >> 18) & 0x1FFu, quirk = r.m1 & 0x1FFu;
+    const uint32_t flags = (r.m1 >> 17) & 0xFu;
+    return !wall && !over && !quirk && !(flags & (SF_INLET | SF_OUTLET));
+}
+
 inline uint64_t special_order_key(int32_t xy)
 {
     const uint64_t x = (uint64_t)(xy & 0xFFFF), y = (uint64_t)((uint32_t)xy >> 16);
@@ -273,17 +283,20 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         L.specials.push_back(rec);
         spec_level.push_back(l);
     }
-    // special records grouped by level, then by whether they have wall links,
-    // then ordered by 8x4 block of sites (row-major blocks, row-major inside a
-    // block), so a warp of the special-cell kernel takes one path over a
-    // compact patch
+    // special records grouped by level, heavy before light, then by whether they
+    // have wall links, then ordered by 8x4 block of sites (row-major blocks,
+    // row-major inside a block), so a warp of the special-cell kernel takes one
+    // path over a compact patch
     {
         std::vector<int64_t> order(L.specials.size());
         for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
         std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
             if (spec_level[a] != spec_level[b]) return spec_level[a] < spec_level[b];
-            // cells with wall links (the longer path) apart from the others, so
-            // the warps of the special-cell kernel take one path
+            // heavy records first, light ones last (the 8x4 plain kernel can take
+            // those); cells with wall links apart from the others, so the warps of
+            // the special-cell kernel take one path
+            const bool la = special_is_light(L.specials[a]), lb = special_is_light(L.specials[b]);
+            if (la != lb) return la < lb;
             const bool wa = ((L.specials[a].m0 >> 18) & 0x1FFu) != 0, wb = ((L.specials[b].m0 >> 18) & 0x1FFu) != 0;
             if (wa != wb) return wa < wb;
             return special_order_key(L.specials[a].xy) < special_order_key(L.specials[b].xy);
@@ -291,13 +304,14 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         std::vector<SpecialRec> sorted(order.size());
         for (size_t i = 0; i < order.size(); i++) sorted[i] = L.specials[order[i]];
         L.specials.swap(sorted);
-        for (auto &lv : L.levels) lv.spec_count = 0;
+        for (auto &lv : L.levels) lv.spec_count = lv.spec_heavy = 0;
         for (size_t i = 0; i < L.specials.size(); i++)
         {
             int l = spec_level[order[i]];
             LevelLayout &lv = L.levels[l - 1];
             if (lv.spec_count == 0) lv.spec_begin = (int64_t)i;
             lv.spec_count++;
+            if (!special_is_light(L.specials[i])) lv.spec_heavy++;
             const int32_t xy = L.specials[i].xy;
             lv.spec[(size_t)(xy >> 16) * lv.pitch + (xy & 0xFFFF)] = (uint32_t)i;
         }
@@ -343,15 +357,16 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
         }
     }
 
-    // 8x4 tiles holding a plain cell, row-major (one warp per tile in the
-    // direct 8x4 kernel; sparse levels fill them better than 32x8 tiles)
+    // 8x4 tiles holding a plain or light cell, row-major (one warp per tile in the
+    // 8x4 kernel: sparse levels fill them better than 32x8 tiles), with the mask
+    // of their light cells
     for (auto &lv : L.levels)
     {
         const int t8x = (lv.W + 7) / 8, t8y = (lv.H + 3) / 4;
         for (int ty = 0; ty < t8y; ty++)
             for (int tx = 0; tx < t8x; tx++)
             {
-                uint32_t m = 0;
+                uint32_t m = 0, light = 0;
                 for (int r = 0; r < 4; r++)
                 {
                     const int yy = ty * 4 + r;
@@ -359,12 +374,21 @@ ImageLayout build_layout(const Grid &g, const LayoutParams &p)
                     for (int k = 0; k < 8; k++)
                     {
                         const int xx = tx * 8 + k;
-                        if (xx < lv.W && lv.omega[(size_t)yy * lv.pitch + xx] > 0.0f) m |= 1u << (8 * r + k);
+                        if (xx >= lv.W) break;
+                        const size_t site = (size_t)yy * lv.pitch + xx;
+                        const float om = lv.omega[site];
+                        if (om > 0.0f) m |= 1u << (8 * r + k);
+                        else if (om < 0.0f && special_is_light(L.specials[lv.spec[site]]))
+                        {
+                            m |= 1u << (8 * r + k);
+                            light |= 1u << (8 * r + k);
+                        }
                     }
                 }
                 if (!m) continue;
                 lv.tile8_list.push_back(tx | ty << 16);
                 lv.tile8_mask.push_back(m);
+                lv.tile8_light.push_back(light);
             }
     }
 

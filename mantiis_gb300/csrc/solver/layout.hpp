@@ -76,11 +76,16 @@ struct LevelLayout
     int n_tiles_interior = 0;        // tiles with tx in [1, tiles_x - 2] (no x wrap within one cell)
     std::vector<uint32_t> tile_mask; // per active tile, 8 row masks of its plain cells (bit = x offset)
     int tiles_x = 0, tiles_y = 0;
-    std::vector<int32_t> tile8_list;  // 8x4 tiles holding a plain cell: tx | ty << 16 (x in 8s, y in 4s)
-    std::vector<uint32_t> tile8_mask; // per such tile, its plain cells (bit = 8 * row + column)
+    std::vector<int32_t> tile8_list;  // 8x4 tiles holding a plain or light cell: tx | ty << 16 (x in 8s, y in 4s)
+    std::vector<uint32_t> tile8_mask; // per such tile, its plain and light cells (bit = 8 * row + column)
+    std::vector<uint32_t> tile8_light;// per such tile, its light cells (subset of tile8_mask)
     int64_t n_active = 0, n_active_real = 0;
     int substeps = 1;                // per coarse step, 2^(L-l)
     int64_t spec_begin = 0, spec_count = 0; // this level's special records (sorted by site)
+    // the first spec_heavy records of the level have wall links, x-periodic
+    // overrides or inlet / outlet roles; the rest ("light": missing arrivals and
+    // buffer status only) can be stepped by the 8x4 plain kernel
+    int64_t spec_heavy = 0;
     bool snapshot_all = false;       // level keeps the coarse-step-start (rho,u) of all cells
 };
 
