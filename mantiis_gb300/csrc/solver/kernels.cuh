@@ -317,6 +317,7 @@ struct PhaseLaunch
 {
     int ndesc;
     int start[kMaxPhaseDescs + 1]; // first block of each descriptor; start[ndesc] = blocks
+    int grid;                      // blocks launched (k_phase_plain8: may be fewer; they loop)
     PhaseArgs a;
     StepDesc d[kMaxPhaseDescs];
 };
@@ -343,20 +344,27 @@ __global__ void __launch_bounds__(256, 5) k_phase_plain(const __grid_constant__ 
     if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
 }
 
-// plain cells in 8x4 tiles: 8 tiles (warps) per block
+// plain cells in 8x4 tiles: 8 tiles (warps) per block-sized unit of work; a
+// block walks units blockIdx.x, blockIdx.x + gridDim.x, ...  Alone the launch
+// has a block per unit; when other images' kernels run beside it (batch
+// streams) it has at most 4 blocks per SM, so they find room on every SM.
 __global__ void __launch_bounds__(256, 5) k_phase_plain8(const __grid_constant__ PhaseLaunch P)
 {
-    const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
-    const StepDesc &d = P.d[j];
-    const int t = ((int)blockIdx.x - P.start[j]) * 8 + (int)(threadIdx.x >> 5);
-    const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
-    double r_diff = 0.0, r_norm = 0.0;
-    if (t < d.L.ntiles8)
+    const int units = P.start[P.ndesc];
+    for (int u = (int)blockIdx.x; u < units; u += (int)gridDim.x)
     {
-        if (d.o.parity) plain_tile8<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
-        else plain_tile8<0>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+        const int j = owner(P.start, P.ndesc, u);
+        const StepDesc &d = P.d[j];
+        const int t = (u - P.start[j]) * 8 + (int)(threadIdx.x >> 5);
+        const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
+        double r_diff = 0.0, r_norm = 0.0;
+        if (t < d.L.ntiles8)
+        {
+            if (d.o.parity) plain_tile8<1>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+            else plain_tile8<0>(d.L, d.C, d.o, t, diff, store_u, r_diff, r_norm);
+        }
+        if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
     }
-    if (diff) block_add2(r_diff, r_norm, d.C.red + P.a.red_slot);
 }
 
 // special cells: blocks of a descriptor walk its records, 128 per block

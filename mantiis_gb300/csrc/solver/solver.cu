@@ -491,9 +491,9 @@ std::unique_ptr<PhasePlan> build_plan(const std::vector<mgpu_ctx *> &ctxs, int o
 std::string state_key(const std::vector<mgpu_ctx *> &ctxs, int ahead);
 PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, int ahead);
 void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaStream_t main, SideLanes &lanes,
-                  int64_t &launches);
+                  int64_t &launches, bool share = false);
 void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, SideLanes &lanes,
-                dev::PhaseArgs a, int64_t &launches);
+                dev::PhaseArgs a, int64_t &launches, bool share = false);
 
 // ---- one coarse time step (include/mantiisApp.hpp:239-246, include/coreLB.hpp:1310-1331)
 void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
@@ -968,6 +968,7 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
         }
         V.plain[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(pl);
         V.plain8[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(p8);
+        for (auto &l : V.plain8[ph]) l.grid = std::min(l.start[l.ndesc], ctxs[0]->sm_count * 4);
         V.spec[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(sp);
         V.tma[ph] = pack_launches<dev::TmaLaunch, dev::StepDesc, dev::kMaxTmaDescs>(tm);
         for (size_t k = 0; k < V.tma[ph].size(); k++)
@@ -1019,8 +1020,13 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
 // The launches of one phase: plain cells on `main` (TMA tiles, direct-load
 // tiles), special cells forked onto `side` (their slot sets are disjoint
 // under the AA ownership rule).
+// share: other images' kernels run beside this phase (batch streams); the 8x4
+// plain kernel then launches at most 4 blocks per SM, which walk its tiles, so
+// the special-cell kernel and the other streams' kernels find room on every SM
+// (config-2 batch +6 %; alone, the full grid is faster: 16.4 against 19.1 us
+// per level-1 substep)
 void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaStream_t main, SideLanes &lanes,
-                  int64_t &launches)
+                  int64_t &launches, bool share)
 {
     const auto &plain = V.plain[ph], &plain8 = V.plain8[ph], &spec = V.spec[ph];
     const auto &tma = V.tma[ph];
@@ -1045,7 +1051,8 @@ void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaSt
     {
         dev::PhaseLaunch l = l0;
         l.a = a;
-        dev::k_phase_plain8<<<(unsigned)l.start[l.ndesc], 256, 0, main>>>(l);
+        const int blocks = l.start[l.ndesc];
+        dev::k_phase_plain8<<<(unsigned)(share ? std::min(blocks, l.grid) : blocks), 256, 0, main>>>(l);
         CK(cudaGetLastError());
         launches++;
     }
@@ -1080,7 +1087,7 @@ void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaSt
 // One coarse step of every image of the group: the phases, then the
 // interface waves.
 void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t main, SideLanes &lanes,
-                dev::PhaseArgs a, int64_t &launches)
+                dev::PhaseArgs a, int64_t &launches, bool share)
 {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(main, &cs));
@@ -1089,7 +1096,7 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     PhaseVariant &V = plan_variant(P, ctxs, 0);
     const dev::PhaseArgs none{0, 0, 0};
     for (int ph = 0; ph < P.nphase; ph++)
-        launch_phase(V, ph, ph == 0 ? a : none, main, lanes, launches);
+        launch_phase(V, ph, ph == 0 ? a : none, main, lanes, launches, share);
     for (int w = 0; w < P.nwave; w++)
         for (const auto &l : V.waves[w])
         {
@@ -2061,7 +2068,7 @@ void batch_step(mgpu_batch *b, int n = 1)
         for (size_t i = 0; i < b->ctxs.size(); i++)
             for (int k = 0; k < n; k++)
                 phase_step(*b->ctxs[i]->plan, {b->ctxs[i]}, b->img_stream[i % ns], b->img_lanes[i % ns], none,
-                           b->launches);
+                           b->launches, ns > 1);
         for (size_t j = 0; j < ns; j++)
         {
             CK(cudaEventRecord(b->img_done[j], b->img_stream[j]));
