@@ -339,7 +339,9 @@ def main():
     assert stream.cuda_stream != 0
     solvers = []
     for img in imgs:
-        s = Solver(img["pore"], img["kn"], img["locpore"], params_for(img, args.plain_path))
+        p_img = params_for(img, args.plain_path)
+        p_img.concurrent = 1  # the batch and the end-to-end leg step several images at once
+        s = Solver(img["pore"], img["kn"], img["locpore"], p_img)
         s.set_stream(stream.cuda_stream)
         solvers.append(s)
     lu_step = float(sum(s.info["lu_per_step"] for s in solvers))
@@ -406,6 +408,7 @@ def main():
     # residual and break test, and the cell fields are read back
     Ke = args.e2e_steps
     e2e_streams = [torch.cuda.Stream() for _ in solvers]
+    # (the contexts were created with concurrent=1: two of them step at once)
     for s, st in zip(solvers, e2e_streams):
         s.set_stream(st.cuda_stream)
 

@@ -61,6 +61,9 @@ typedef struct mgpu_params
                               tiles, one warp each (fits sparse levels better); -1 (default) = pick the
                               fastest per image by timing all three over a few coarse steps at creation
                               (the state is put back; results are bit-identical on every path) */
+    int concurrent;        /* 1: other contexts step on this GPU at the same time (several host threads or
+                              streams); the 8x4 plain kernel then leaves room on every SM for their kernels
+                              (a batch does this by itself).  0 (default): this context has the GPU */
 } mgpu_params;
 
 /* Static description of a built context. */

@@ -563,7 +563,7 @@ void coarse_step(mgpu_ctx *ctx, bool diff, bool store_u, int red_slot)
         return;
     }
     dev::PhaseArgs a{diff ? 1 : 0, store_u ? 1 : 0, red_slot};
-    phase_step(*ctx->plan, {ctx}, ctx->stream, ctx->lanes, a, ctx->launches);
+    phase_step(*ctx->plan, {ctx}, ctx->stream, ctx->lanes, a, ctx->launches, ctx->prm.concurrent != 0);
 }
 
 // read pass over all reference cells
@@ -1124,6 +1124,9 @@ void autotune_plain_path(mgpu_ctx *ctx)
     CK(cudaEventCreate(&e1));
     checkpoint_save(ctx);
     const int64_t launches0 = ctx->launches;
+    // the paths are timed with the GPU to themselves
+    const int concurrent = ctx->prm.concurrent;
+    ctx->prm.concurrent = 0;
     double us[3] = {0.0, 0.0, 0.0};
     auto select = [&](int path) {
         for (size_t l = 0; l < ctx->lv.size(); l++)
@@ -1156,6 +1159,7 @@ void autotune_plain_path(mgpu_ctx *ctx)
     select(best);
     for (int path = 0; path < 3; path++) ctx->autotune_us[path] = us[path];
     ctx->launches = launches0;
+    ctx->prm.concurrent = concurrent;
     checkpoint_release(ctx);
 }
 
@@ -1192,6 +1196,7 @@ void mgpu_default_params(mgpu_params *p)
     p->check_every = 1;
     p->edge_fine = 0;
     p->plain_path = -1;
+    p->concurrent = 0;
 }
 
 static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **out)

@@ -38,6 +38,7 @@ class Params(C.Structure):
         ("check_every", C.c_int),
         ("edge_fine", C.c_int),
         ("plain_path", C.c_int),
+        ("concurrent", C.c_int),
     ]
 
 
