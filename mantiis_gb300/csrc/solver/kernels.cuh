@@ -367,12 +367,16 @@ __global__ void __launch_bounds__(256, 5) k_phase_plain8(const __grid_constant__
     }
 }
 
-// special cells: blocks of a descriptor walk its records, 128 per block
-__global__ void __launch_bounds__(128) k_phase_special(const __grid_constant__ PhaseLaunch P)
+// special cells: blocks of a descriptor walk its records, kSpecialBlock per block
+// special records per block of k_phase_special (64 and 32 measured slower: config-2
+// batch 338 / 343 / 353 us per coarse step for 128 / 64 / 32)
+constexpr int kSpecialBlock = 128;
+
+__global__ void __launch_bounds__(kSpecialBlock) k_phase_special(const __grid_constant__ PhaseLaunch P)
 {
     const int j = owner(P.start, P.ndesc, (int)blockIdx.x);
     const StepDesc &d = P.d[j];
-    const int i = ((int)blockIdx.x - P.start[j]) * 128 + (int)threadIdx.x;
+    const int i = ((int)blockIdx.x - P.start[j]) * kSpecialBlock + (int)threadIdx.x;
     const int diff = P.a.diff & d.o.first_sub, store_u = P.a.store_u & d.o.first_sub;
     double r_diff = 0.0, r_norm = 0.0;
     if (i < d.spec_count)

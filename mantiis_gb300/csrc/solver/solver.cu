@@ -964,7 +964,7 @@ PhaseVariant &plan_variant(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, in
             // special-cell kernel takes the level's heavy prefix only
             const int nspec = (int)(c->lv[l].use8 ? ll.spec_heavy : ll.spec_count);
             sd.spec_count = nspec;
-            if (nspec) sp.push_back({sd, (nspec + 127) / 128});
+            if (nspec) sp.push_back({sd, (nspec + dev::kSpecialBlock - 1) / dev::kSpecialBlock});
         }
         V.plain[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(pl);
         V.plain8[ph] = pack_launches<dev::PhaseLaunch, dev::StepDesc, dev::kMaxPhaseDescs>(p8);
@@ -1068,7 +1068,8 @@ void launch_phase(const PhaseVariant &V, int ph, const dev::PhaseArgs &a, cudaSt
     {
         dev::PhaseLaunch l = l0;
         l.a = a;
-        dev::k_phase_special<<<(unsigned)l.start[l.ndesc], 128, 0, special_side ? lanes.special : main>>>(l);
+        dev::k_phase_special<<<(unsigned)l.start[l.ndesc], dev::kSpecialBlock, 0,
+                               special_side ? lanes.special : main>>>(l);
         CK(cudaGetLastError());
         launches++;
     }
