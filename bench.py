@@ -464,7 +464,10 @@ def main():
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
                        "l2": "inputs larger than L2 (state of the batch > 129 MB)",
                        "graph": "one CUDA graph of 2 coarse steps for the whole batch, images on L2-sized concurrent streams",
-                       "state_finite_after_timed_steps": finite},
+                       "state_finite_after_timed_steps": finite,
+                       **({} if finite else {"state_note": "the reference's multi-block scheme diverges on these "
+                                                           "images (its FP64 restatement too); the step's work "
+                                                           "and timing do not depend on the values"})},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": f"level-1 substep ({plain_kernels} + k_phase_special)", "units_per_launch": lvl1["active"],
