@@ -13,8 +13,10 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
   refstate_coupled64.npz  the reference's coupled run on the 64x64 test image
   refprops.npz      local pore size and Kn from the reference's own
                     Shape::calculateProperties on four pore images
+  refprops_extra.npz  the same on three irregular images (noise, blobs,
+                    diagonal channels)
 
-Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|coupled]
+Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|coupled]
 """
 import os
 import struct
@@ -223,11 +225,38 @@ def properties_fixture(fx):
         out[f"{name}_locpore"] = lp
         out[f"{name}_kn"] = kn
     np.savez_compressed(HERE / "refprops.npz", dx=1e-9, mfp=5e-9, **out)
+    properties_extra_fixture()
+
+
+def properties_extra_fixture():
+    """Three irregular images for the host pipeline: salt-and-pepper noise (many
+    one-pixel pores and tiny components), smoothed random blobs, and thin
+    diagonal channels (skeletons that are all diagonal steps)."""
+    rng = np.random.default_rng(17)
+    images = {"noise96": (rng.random((96, 96)) < 0.58).astype(np.int32)}
+    field = rng.random((128, 128))
+    for _ in range(6):  # smoothing by neighbour averages on the torus
+        field = (field + np.roll(field, 1, 0) + np.roll(field, -1, 0) + np.roll(field, 1, 1)
+                 + np.roll(field, -1, 1)) / 5.0
+    images["blobs128"] = (field > np.median(field)).astype(np.int32)
+    y, x = np.mgrid[0:128, 0:128]
+    images["diagonal128"] = (((x + y) % 24) < 5).astype(np.int32)
+    for im in images.values():
+        im[0, :] = 0
+        im[-1, :] = 0
+    out = {}
+    for name, pore in images.items():
+        lp, kn = run_ref_properties(pore, 1e-9, 5e-9)
+        out[f"{name}_pore"] = pore.astype(np.uint8)
+        out[f"{name}_locpore"] = lp
+        out[f"{name}_kn"] = kn
+    np.savez_compressed(HERE / "refprops_extra.npz", dx=1e-9, mfp=5e-9, **out)
 
 
 if __name__ == "__main__":
     if _ONLY:
         fx = dict(np.load(HERE / "fixture64.npz"))
-        {"properties": properties_fixture, "coupled": coupled_fixture}[_ONLY](fx)
+        {"properties": properties_fixture, "coupled": coupled_fixture,
+         "properties_extra": lambda _: properties_extra_fixture()}[_ONLY](fx)
     else:
         main()

@@ -43,3 +43,15 @@ def test_solid_pixels_get_zero(refprops):
 def test_too_small_image_rejected():
     with pytest.raises(MantiisError):
         pore_properties(np.ones((3, 3), np.int32), 1e-9, 5e-9)
+
+
+EXTRA = ("noise96", "blobs128", "diagonal128")
+
+
+@pytest.mark.parametrize("name", EXTRA)
+def test_host_properties_match_reference_irregular(name):
+    # salt-and-pepper noise, smoothed blobs, thin diagonal channels
+    ref = load("refprops_extra.npz")
+    pore = ref[f"{name}_pore"].astype(np.int32)
+    lp, kn = pore_properties(pore, float(ref["dx"]), float(ref["mfp"]))
+    check_against_reference(lp, kn, ref, name)
