@@ -15,8 +15,10 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
                     Shape::calculateProperties on four pore images
   refprops_extra.npz  the same on three irregular images (noise, blobs,
                     diagonal channels)
+  refstate_config1_200.npz  the reference's own run on the config-1 disk image
+                    (128x128, single block), cell fields after 200 steps
 
-Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|coupled]
+Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|disk_state|coupled]
 """
 import os
 import struct
@@ -165,6 +167,7 @@ def main():
                                 **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
     coupled_fixture(fx)
     properties_fixture(fx)
+    disk_state_fixture()
     print("fixtures written to", HERE)
 
 
@@ -178,6 +181,26 @@ def coupled_fixture(fx):
         grid, states = run_ref(f, 64, 30, False, mode="coupled", dx=12e-9, dump_steps=(100, 101, 130))
         np.savez_compressed(HERE / "refstate_coupled64.npz",
                             **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
+
+
+def disk_state_fixture():
+    """The reference's own single-block run on the config-1 disk image
+    (128x128, radii U[4,10], porosity 0.65, Kn ~0.1, the package's seeded
+    generator and its dx): cell fields after 200 steps."""
+    sys.path.insert(0, str(ROOT))
+    from mantiis_gb300 import workloads
+
+    img = workloads.config1(0)
+    # the values as the reference reads them back from the %.6e text files
+    kn = np.vectorize(lambda v: float(f"{v:.6e}"))(img["kn"])
+    lp = np.vectorize(lambda v: float(f"{v:.6e}"))(img["locpore"])
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "c1"
+        write_col_major(f, img["pore"], kn, lp)
+        _, states = run_ref(f, 128, 200, False, dx=img["dx"], dump_steps=(200,))
+    st = states[200]
+    np.savez_compressed(HERE / "refstate_config1_200.npz", pore=img["pore"].astype(np.uint8), kn=kn, locpore=lp,
+                        dx=img["dx"], rho=st["rho"], ux=st["ux"], uy=st["uy"], residuals=st["residuals"])
 
 
 def run_ref_properties(pore, dx, mfp):
@@ -257,6 +280,7 @@ if __name__ == "__main__":
     if _ONLY:
         fx = dict(np.load(HERE / "fixture64.npz"))
         {"properties": properties_fixture, "coupled": coupled_fixture,
-         "properties_extra": lambda _: properties_extra_fixture()}[_ONLY](fx)
+         "properties_extra": lambda _: properties_extra_fixture(),
+         "disk_state": lambda _: disk_state_fixture()}[_ONLY](fx)
     else:
         main()

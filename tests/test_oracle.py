@@ -78,3 +78,19 @@ def test_oracle_coupled_run_matches_reference_code(fixture64):
             assert np.abs(f["ux"] - st[f"ux_{step}"]).max() < 1e-10
             assert np.abs(f["rho"] - st[f"rho_{step}"]).max() < 1e-10
     assert np.allclose(o.residuals()[100:], 1.0)
+
+
+def test_oracle_matches_reference_on_disk_image():
+    # the config-1 disk image (128x128, single block, Kn ~0.1): the reference's
+    # own code (refstate_config1_200.npz) after 200 steps
+    st = load("refstate_config1_200.npz")
+    pore = st["pore"].astype(np.int32)
+    dx = float(st["dx"])
+    g = HostGrid(pore, st["kn"], st["locpore"], default_params(dx=dx))
+    o = for_grid(g, sim="transport", dx=dx)
+    assert o.run(200) == 200
+    f = o.fields()
+    for name in ("rho", "ux", "uy"):
+        scale = np.abs(st[name]).max()
+        assert np.abs(f[name] - st[name]).max() <= 1e-12 * scale, name
+    assert np.allclose(o.residuals(), st["residuals"], rtol=1e-9, atol=0)
