@@ -17,8 +17,10 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
                     diagonal channels)
   refstate_config1_200.npz  the reference's own run on the config-1 disk image
                     (128x128, single block), cell fields after 200 steps
+  refstate_adsorption128_100.npz  the reference's own adsorption run on a
+                    128x128 disk image, cell fields after 100 steps
 
-Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|disk_state|coupled]
+Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|disk_state|disk_adsorption|coupled]
 """
 import os
 import struct
@@ -168,6 +170,7 @@ def main():
     coupled_fixture(fx)
     properties_fixture(fx)
     disk_state_fixture()
+    disk_adsorption_fixture()
     print("fixtures written to", HERE)
 
 
@@ -201,6 +204,25 @@ def disk_state_fixture():
     st = states[200]
     np.savez_compressed(HERE / "refstate_config1_200.npz", pore=img["pore"].astype(np.uint8), kn=kn, locpore=lp,
                         dx=img["dx"], rho=st["rho"], ux=st["ux"], uy=st["uy"], residuals=st["residuals"])
+
+
+def disk_adsorption_fixture():
+    """The reference's own adsorption run (PR-EOS pseudopotential, bounce-back
+    walls, inlet/outlet) on a 128x128 seeded disk image at dx = 12 nm: cell
+    fields after 100 steps."""
+    sys.path.insert(0, str(ROOT))
+    from mantiis_gb300 import workloads
+
+    img = workloads.image(128, 6, 14, 0.6, 0.1, 3100)
+    kn = np.vectorize(lambda v: float(f"{v:.6e}"))(img["kn"])
+    lp = np.vectorize(lambda v: float(f"{v:.6e}"))(img["locpore"])
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "a1"
+        write_col_major(f, img["pore"], kn, lp)
+        _, states = run_ref(f, 128, 100, False, mode="adsorption", dx=12e-9, dump_steps=(100,))
+    st = states[100]
+    np.savez_compressed(HERE / "refstate_adsorption128_100.npz", pore=img["pore"].astype(np.uint8), kn=kn,
+                        locpore=lp, rho=st["rho"], ux=st["ux"], uy=st["uy"], residuals=st["residuals"])
 
 
 def run_ref_properties(pore, dx, mfp):
@@ -281,6 +303,7 @@ if __name__ == "__main__":
         fx = dict(np.load(HERE / "fixture64.npz"))
         {"properties": properties_fixture, "coupled": coupled_fixture,
          "properties_extra": lambda _: properties_extra_fixture(),
-         "disk_state": lambda _: disk_state_fixture()}[_ONLY](fx)
+         "disk_state": lambda _: disk_state_fixture(),
+         "disk_adsorption": lambda _: disk_adsorption_fixture()}[_ONLY](fx)
     else:
         main()

@@ -94,3 +94,19 @@ def test_oracle_matches_reference_on_disk_image():
         scale = np.abs(st[name]).max()
         assert np.abs(f[name] - st[name]).max() <= 1e-12 * scale, name
     assert np.allclose(o.residuals(), st["residuals"], rtol=1e-9, atol=0)
+
+
+def test_oracle_adsorption_matches_reference_on_disk_image():
+    # PR-EOS pseudopotential, bounce-back walls and the inlet/outlet on a 128x128
+    # seeded disk image at dx = 12 nm: the reference's own run after 100 steps
+    from mantiis_gb300 import SIM_ADSORPTION
+
+    st = load("refstate_adsorption128_100.npz")
+    p = default_params(dx=12e-9, simulation=SIM_ADSORPTION)
+    g = HostGrid(st["pore"].astype(np.int32), st["kn"], st["locpore"], p)
+    o = for_grid(g, sim="adsorption", dx=12e-9)
+    assert o.run(100) == 100
+    f = o.fields()
+    for name in ("rho", "ux", "uy"):
+        assert np.abs(f[name] - st[name]).max() <= 1e-12 * np.abs(st[name]).max(), name
+    assert np.allclose(o.residuals(), st["residuals"], rtol=1e-9, atol=0)
