@@ -122,3 +122,18 @@ def test_config3_full_size_vs_oracle():
     record("config3_512_200", rho=e_rho, mass=abs(m_gpu - m_ref) / m_ref, drift_ref=abs(m_ref - m0) / m0,
            rho_span=float(ref["rho"].max() - ref["rho"].min()))
     assert e_rho < 1e-5 and abs(m_gpu - m_ref) / m_ref < 1e-6
+
+
+def test_adsorption_disk_image_vs_reference_code():
+    # a 128x128 disk image against the reference's own adsorption run
+    # (refstate_adsorption128_100.npz): PR-EOS psi, BB walls, inlet/outlet, 100 steps
+    st = load("refstate_adsorption128_100.npz")
+    p = default_params(dx=12e-9, simulation=SIM_ADSORPTION, tol=0.0)
+    s = Solver(st["pore"].astype(np.int32), st["kn"], st["locpore"], p)
+    assert s.run(100) == 100
+    c = s.cells()
+    umax = np.abs(st["ux"]).max()
+    e_ux = np.abs(c["ux"] - st["ux"]).max() / umax
+    e_rho = np.abs(c["rho"] - st["rho"]).max() / np.abs(st["rho"]).max()
+    record("adsorption_disk128_vs_reference_100", ux=e_ux, rho=e_rho)
+    assert e_ux < 1e-3 and e_rho < 1e-4

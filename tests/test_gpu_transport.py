@@ -279,3 +279,17 @@ def test_config1_permeability_vs_oracle():
     e = abs(k_gpu - k_ref) / abs(k_ref)
     record("config1_permeability_5000", rel=e, k=k_gpu)
     assert e < 1e-5
+
+
+def test_disk_image_vs_reference_code():
+    # the config-1 disk image (disks crossing the x-periodic seam) against the
+    # reference's own run (refstate_config1_200.npz): 200 steps, FP32 GPU
+    st = load("refstate_config1_200.npz")
+    p = default_params(dx=float(st["dx"]), tol=0.0)
+    s = Solver(st["pore"].astype(np.int32), st["kn"], st["locpore"], p)
+    assert s.run(200) == 200
+    c = s.cells()
+    e_ux = rel_err(c["ux"], st["ux"])
+    e_rho = np.abs(c["rho"] - st["rho"]).max() / np.abs(st["rho"]).max()
+    record("config1_disk_vs_reference_200", ux=e_ux, rho=e_rho)
+    assert e_ux < 1e-5 and e_rho < 1e-6
