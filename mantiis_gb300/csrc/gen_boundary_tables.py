@@ -9,6 +9,7 @@ boundary type (52); icsr is 1-based in the file.
 
 Usage: python gen_boundary_tables.py <system_files_dir> > boundary_tables.h
 """
+import os
 import sys
 
 
@@ -56,4 +57,10 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include/system_files")
+    # the reference's include/system_files folder: first argument or $MANTIIS_REF_DIR/include/system_files
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("MANTIIS_REF_DIR"):
+        main(os.path.join(os.environ["MANTIIS_REF_DIR"], "include", "system_files"))
+    else:
+        sys.exit("usage: gen_boundary_tables.py <reference>/include/system_files  (or set MANTIIS_REF_DIR)")

@@ -1913,26 +1913,54 @@ __device__ __align__(256) double g_noalloc_stage[3 * (size_t)MGPU_NOALLOC_MAX_CE
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[kMaxDevices] = {};
+struct NoallocSlot
+{
+    unsigned long long context_id = 0; // CUDA context the address belongs to (0 = none yet)
+    double *ptr = nullptr;
+};
+NoallocSlot g_noalloc_slot[kMaxDevices];
 
-// the array's device address on `device`, looked up once per device with that
-// device current (the first lookup may load the module)
+// Process-unique id of the CUDA context bound to the calling thread (cuCtxGetId,
+// through the runtime's entry-point query).  Ids are never reused, unlike context
+// handles: a primary context re-created after cudaDeviceReset gets a new id.
+// Returns false when no context is bound to the thread yet.
+bool current_context_id(unsigned long long *id)
+{
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    if (!get_current || !get_id)
+    {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1 = cudaDriverEntryPointSymbolNotFound, r2 = r1;
+        CK(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &r1));
+        CK(cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2));
+        if (r1 != cudaDriverEntryPointSuccess || r2 != cudaDriverEntryPointSuccess || !p || !q)
+            throw CudaError("cuCtxGetCurrent / cuCtxGetId are not available");
+        get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(q);
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return false;
+    return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// The array's device address in the context current on `device`.  It is looked
+// up (cudaGetSymbolAddress, which may load the module) once per CUDA context and
+// kept with that context's id, so a context created after cudaDeviceReset, whose
+// module may sit at another address, gets its own lookup.
 double *noalloc_stage(int device)
 {
     if (device < 0 || device >= kMaxDevices) throw std::invalid_argument("device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device])
-    {
-        int prev = -1;
-        CK(cudaGetDevice(&prev));
-        if (prev != device) CK(cudaSetDevice(device));
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_stage);
-        if (prev != device) CK(cudaSetDevice(prev));
-        CK(e);
-        g_noalloc_ptr[device] = static_cast<double *>(p);
-    }
-    return g_noalloc_ptr[device];
+    NoallocSlot &s = g_noalloc_slot[device];
+    unsigned long long id = 0;
+    if (current_context_id(&id) && s.ptr && s.context_id == id) return s.ptr;
+    void *p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_stage)); // binds the device's primary context to this thread
+    if (!current_context_id(&id)) throw CudaError("no CUDA context is current after cudaGetSymbolAddress");
+    s.context_id = id;
+    s.ptr = static_cast<double *>(p);
+    return s.ptr;
 }
 } // namespace
 

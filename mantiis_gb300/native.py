@@ -284,12 +284,18 @@ class Solver:
         if rc != 0:
             raise MantiisError(rc, L.mgpu_global_error().decode())
         self._h = h
-        inf = Info()
-        L.mgpu_get_info(h, C.byref(inf))
-        self.info = {f: getattr(inf, f) for f, _ in Info._fields_ if f != "pad_"}
-        self.info["autotune_us"] = tuple(self.info["autotune_us"])
+        self.refresh_info()
         self.n = self.info["n"]
         self.n_cells = self.info["n_cells"]
+
+    def refresh_info(self):
+        """Re-reads mgpu_get_info (device_bytes grows when buffers are created on
+        first use, e.g. by set_equilibrium) into self.info and returns it."""
+        inf = Info()
+        self._check(lib().mgpu_get_info(self._h, C.byref(inf)))
+        self.info = {f: getattr(inf, f) for f, _ in Info._fields_ if f != "pad_"}
+        self.info["autotune_us"] = tuple(self.info["autotune_us"])
+        return self.info
 
     def _check(self, rc):
         if rc != 0:
@@ -378,9 +384,15 @@ class Solver:
         self._check(lib().mgpu_reconstructed(self._h, out))
         return out.reshape(self.n, self.n)
 
-    def set_equilibrium(self, rho, ux, uy):
+    def _cell_fields(self, rho, ux, uy):
         a = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in (rho, ux, uy)]
-        self._check(lib().mgpu_set_equilibrium(self._h, *a))
+        for name, v in zip(("rho", "ux", "uy"), a):
+            if v.size != self.n_cells:
+                raise ValueError(f"{name} holds {v.size} values, expected n_cells = {self.n_cells}")
+        return a
+
+    def set_equilibrium(self, rho, ux, uy):
+        self._check(lib().mgpu_set_equilibrium(self._h, *self._cell_fields(rho, ux, uy)))
 
     def set_distributions(self, f, layout="cells", t=0):
         """Restart from populations (mgpu_set_distributions): f of
@@ -395,8 +407,7 @@ class Solver:
     def set_equilibrium_noalloc(self, rho, ux, uy):
         """set_equilibrium staged through the library's static device array
         (mgpu_set_equilibrium_noalloc): no allocation, at most NOALLOC_MAX_CELLS cells."""
-        a = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in (rho, ux, uy)]
-        self._check(lib().mgpu_set_equilibrium_noalloc(self._h, *a))
+        self._check(lib().mgpu_set_equilibrium_noalloc(self._h, *self._cell_fields(rho, ux, uy)))
 
     def set_stream(self, stream_handle):
         self._check(lib().mgpu_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))

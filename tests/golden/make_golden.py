@@ -19,8 +19,11 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
                     (128x128, single block), cell fields after 200 steps
   refstate_adsorption128_100.npz  the reference's own adsorption run on a
                     128x128 disk image, cell fields after 100 steps
+  refstate_variants.npz  the reference's own runs with BGK / MRT collisions and
+                    MDBB / BB walls, single block (64x64 test image) and
+                    multi-block (block64 geometry)
 
-Usage: python tests/golden/make_golden.py [REF_DIR] [--only properties|properties_extra|disk_state|disk_adsorption|coupled]
+Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants]
 """
 import os
 import struct
@@ -37,7 +40,9 @@ _ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
 _ONLY = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
 if _ONLY:
     _ARGS.remove(_ONLY)
-REF = Path(_ARGS[0] if _ARGS else "/root/reference")
+if not _ARGS and not os.environ.get("MANTIIS_REF_DIR"):
+    sys.exit("usage: make_golden.py <reference checkout> [--only ...]  (or set MANTIIS_REF_DIR)")
+REF = Path(_ARGS[0] if _ARGS else os.environ["MANTIIS_REF_DIR"])
 DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
 HOME = ROOT / "oracle" / "_ref" / "home"
 
@@ -104,13 +109,14 @@ def read_state(path):
     return s
 
 
-def run_ref(folder, n, steps, multiblock, mode="transport", dx=1e-9, levels=2, dump_steps=()):
+def run_ref(folder, n, steps, multiblock, mode="transport", dx=1e-9, levels=2, dump_steps=(), extra=()):
     exe = DRIVER if levels == 2 else ROOT / "oracle" / "_ref" / "ref_driver3"
     with tempfile.TemporaryDirectory() as dump:
         cmd = [str(exe), "1", "true" if multiblock else "False", str(n), str(folder) + "/", str(steps), "--mode", mode,
                "--dx", repr(dx), "--quiet", "--no-break", "--dump", dump]
         if dump_steps:
             cmd += ["--dump-steps", ",".join(str(s) for s in dump_steps)]
+        cmd += [str(a) for a in extra]
         env = dict(os.environ, HOME=str(HOME))
         subprocess.run(cmd, check=True, env=env, stdout=subprocess.DEVNULL)
         grid = read_grid(Path(dump) / "grid.bin")
@@ -171,6 +177,7 @@ def main():
     properties_fixture(fx)
     disk_state_fixture()
     disk_adsorption_fixture()
+    variants_fixture(fx)
     print("fixtures written to", HERE)
 
 
@@ -184,6 +191,36 @@ def coupled_fixture(fx):
         grid, states = run_ref(f, 64, 30, False, mode="coupled", dx=12e-9, dump_steps=(100, 101, 130))
         np.savez_compressed(HERE / "refstate_coupled64.npz",
                             **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
+
+
+# (collision, wall): 0 BGK, 1 MRT, 2 regularized MRT; 0 BB, 1 MDBB, 2 SRBB
+VARIANTS_SB = [(2, 1), (1, 2), (0, 0), (1, 1), (0, 2), (0, 1)]
+VARIANTS_MB = [(2, 1), (0, 2), (0, 1)]
+
+
+def variants_fixture(fx):
+    """The reference's own runs with the other collision operators and walls
+    (Settings::collision_method / wall_boundary: SRTCollision, include/coreLB.hpp:678-691,
+    MRTCollisionNonRegularized :694-742, MDBBWall :936-967, BBWall :859-865):
+    single block on the 64x64 test image (100 steps) and multi-block on the
+    block64 geometry (50 steps); cell fields and populations at the last step."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "fx64"
+        write_col_major(f, fx["pore"], fx["kn"], fx["locpore"])
+        for c, w in VARIANTS_SB:
+            _, st = run_ref(f, 64, 100, False, dump_steps=(100,), extra=("--collision", c, "--wall", w))
+            for k in ("rho", "ux", "uy", "f"):
+                out[f"sb_c{c}_w{w}_{k}"] = st[100][k]
+        n, wall, obst = CASES["block64"]
+        p, kn, lp = block_geometry(n, wall, obst)
+        f = Path(tmp) / "block64"
+        write_col_major(f, p, kn, lp)
+        for c, w in VARIANTS_MB:
+            _, st = run_ref(f, n, 50, True, dump_steps=(50,), extra=("--collision", c, "--wall", w))
+            for k in ("rho", "ux", "uy", "f"):
+                out[f"mb_c{c}_w{w}_{k}"] = st[50][k]
+    np.savez_compressed(HERE / "refstate_variants.npz", **out)
 
 
 def disk_state_fixture():
@@ -304,6 +341,7 @@ if __name__ == "__main__":
         {"properties": properties_fixture, "coupled": coupled_fixture,
          "properties_extra": lambda _: properties_extra_fixture(),
          "disk_state": lambda _: disk_state_fixture(),
-         "disk_adsorption": lambda _: disk_adsorption_fixture()}[_ONLY](fx)
+         "disk_adsorption": lambda _: disk_adsorption_fixture(),
+         "variants": variants_fixture}[_ONLY](fx)
     else:
         main()

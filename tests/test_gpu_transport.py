@@ -192,6 +192,33 @@ def test_collision_and_wall_variants_vs_oracle(fixture64, collision, wall, multi
     assert e < 1e-4 and e_f < 1e-6
 
 
+VARIANTS_SB = [(2, 1), (1, 2), (0, 0), (1, 1), (0, 2), (0, 1)]
+VARIANTS_MB = [(2, 1), (0, 2), (0, 1)]
+
+
+@pytest.mark.parametrize("collision,wall,multiblock", [(c, w, 0) for c, w in VARIANTS_SB] +
+                         [(c, w, 1) for c, w in VARIANTS_MB])
+def test_variants_vs_reference_code(fixture64, collision, wall, multiblock):
+    # BGK / MRT collisions and MDBB / BB walls against the reference's own runs
+    # (refstate_variants.npz, oracle/_ref): single block on the 64x64 test image
+    # for 100 steps, multi-block on the block64 geometry for 50 steps
+    st = load("refstate_variants.npz")
+    key = f"{'mb' if multiblock else 'sb'}_c{collision}_w{wall}"
+    if multiblock:
+        ref = load("refgrid_block64.npz")
+        img, steps = (ref["img_pore"], ref["img_kn"], ref["img_locpore"]), 50
+    else:
+        img, steps = (fixture64["pore"], fixture64["kn"], fixture64["locpore"]), 100
+    s = Solver(*img, default_params(dx=1e-9, multiblock=multiblock, collision=collision, wall=wall, tol=0.0))
+    assert s.run(steps) == steps
+    got = s.cells(with_f=True)
+    e_ux = rel_err(got["ux"], st[f"{key}_ux"])
+    e_uy = np.abs(got["uy"] - st[f"{key}_uy"]).max() / np.abs(st[f"{key}_ux"]).max()
+    e_f = np.abs(got["f"] - st[f"{key}_f"].reshape(-1, 9)).max() / 0.2355
+    record(f"variant_ref_{key}", ux=e_ux, uy=e_uy, f=e_f)
+    assert e_ux < 1e-4 and e_uy < 1e-4 and e_f < 1e-6
+
+
 def test_plain_paths_agree_and_autotune():
     # the TMA pipeline, the direct 32x8 tiles and the direct 8x4 warp tiles run
     # the same arithmetic on the same slots: bit-identical states; plain_path -1

@@ -33,28 +33,61 @@ def test_max_cells_matches_header():
     assert m and NOALLOC_MAX_CELLS == 1 << int(m.group(1))
 
 
+def test_cell_field_sizes_checked_before_any_call():
+    # short arrays would make the C side read past them: the binding refuses
+    s = Solver.__new__(Solver)
+    s._h, s.n_cells = None, 10
+    ok, short = np.zeros(10), np.zeros(9)
+    for fn in (s.set_equilibrium, s.set_equilibrium_noalloc):
+        with pytest.raises(ValueError, match="expected n_cells = 10"):
+            fn(ok, short, ok)
+
+
 @pytest.mark.gpu
 def test_noalloc_matches_set_equilibrium_twice(fixture64):
+    import torch
+
     # multi-block: the kernel also fills the interface buffers
     p = default_params(dx=1e-9, multiblock=1)
     img = (fixture64["pore"], fixture64["kn"], fixture64["locpore"])
-    ref, got, other = Solver(*img, p), Solver(*img, p), Solver(*img, p)
+    ref, got, other, other_ref = Solver(*img, p), Solver(*img, p), Solver(*img, p), Solver(*img, p)
     n = ref.n_cells
+    # set_equilibrium creates its staging buffers on first use; do that before
+    # the device's free memory is read
+    ref.set_equilibrium(*fields(n, 0))
+    other_ref.set_equilibrium(*fields(n, 0))
+    bytes_before = [s.refresh_info()["device_bytes"] for s in (got, other)]
+
+    def noalloc(s, fl):
+        # the device's free memory is the same before and after the call
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
+        s.set_equilibrium_noalloc(*fl)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free_before
+
     for seed in (1, 2):  # two calls in a row on the same context
         fl = fields(n, seed)
+        noalloc(got, fl)
         ref.set_equilibrium(*fl)
-        got.set_equilibrium_noalloc(*fl)
         e_f, e_ux = state_err(ref, got)
         assert e_f < 1e-6 and e_ux < 1e-4
         ref.advance(10)
         got.advance(10)
         e_f, e_ux = state_err(ref, got)
         assert e_f < 1e-6 and e_ux < 1e-4
-    # a second context on the same device reuses the staging array; the first
-    # context's state is its own
-    other.set_equilibrium_noalloc(*fields(n, 3))
+    # a second context on the same device reuses the staging array: its state
+    # matches set_equilibrium's on the same fields, and the first context's
+    # state is still its own
+    fl = fields(n, 3)
+    noalloc(other, fl)
+    other_ref.set_equilibrium(*fl)
+    e_f, e_ux = state_err(other_ref, other)
+    assert e_f < 1e-6 and e_ux < 1e-4
     e_f, _ = state_err(ref, got)
     assert e_f < 1e-6
+    # and the contexts hold no more device memory than before
+    assert [s.refresh_info()["device_bytes"] for s in (got, other)] == bytes_before
 
 
 @pytest.mark.gpu
