@@ -25,7 +25,8 @@ def test_adsorption_gold_64(fixture64):
     e_uy = np.abs(px["uy"] - fixture64["adsorption_uy"]).max() / umax
     e_rho = np.abs(px["rho"] - fixture64["adsorption_rho"]).max() / np.abs(fixture64["adsorption_rho"]).max()
     record("adsorption_gold_64", ux=e_ux, uy=e_uy, rho=e_rho)
-    assert e_ux < 1e-3 and e_uy < 1e-3 and e_rho < 1e-4
+    # measured on a GB300: u_x 1.0e-6, u_y 2.3e-6, rho 1.3e-6
+    assert e_ux < 1e-5 and e_uy < 2.5e-5 and e_rho < 1.5e-5
 
 
 def test_adsorption_residuals_vs_oracle(fixture64):
@@ -40,7 +41,7 @@ def test_adsorption_residuals_vs_oracle(fixture64):
     assert len(r) == 60 and r[0] == 1e-5 == ref[0]
     e = np.abs(r - ref) / ref
     record("adsorption_residuals_64", max_rel=e.max(), median_rel=np.median(e))
-    assert np.median(e) < 1e-3
+    assert np.median(e) < 2e-5  # measured median 1.6e-6 (max 1.4e-5)
 
 
 def test_exponential_pseudopotential_vs_oracle():
@@ -68,7 +69,9 @@ def test_exponential_pseudopotential_vs_oracle():
     e_rho = np.abs(got["rho"] - ref["rho"]).max() / 0.5
     e_ux = np.abs(got["ux"] - ref["ux"]).max() / max(np.abs(ref["ux"]).max(), 1e-30)
     record("adsorption_exponential_128", rho=e_rho, ux=e_ux)
-    assert e_rho < 1e-6 and e_ux < 1e-3
+    # measured rho 5.9e-8; u (no body force: a weak flow of the density
+    # noise, relative to its own small maximum) 5.1e-4
+    assert e_rho < 6e-7 and e_ux < 5e-3
 
 
 def test_coupled_run_matches_reference_code(fixture64):
@@ -90,7 +93,8 @@ def test_coupled_run_matches_reference_code(fixture64):
         e_ux = np.abs(c["ux"] - st[f"ux_{step}"]).max() / umax if step > 100 else 0.0
         e_rho = np.abs(c["rho"] - st[f"rho_{step}"]).max() / np.abs(st[f"rho_{step}"]).max() if step > 100 else 0.0
         record(f"coupled_64_{step}", f=e_f, ux=e_ux, rho=e_rho)
-        assert e_f < 1e-5 and e_ux < 1e-3 and e_rho < 1e-4
+        # measured (worst step): f 3.3e-6, u_x 1.1e-6, rho 1.2e-6
+        assert e_f < 3.5e-5 and e_ux < 1.2e-5 and e_rho < 1.5e-5
     r = s.residuals()
     assert len(r) == 130 and np.allclose(r[100:], 1.0)
 
@@ -121,7 +125,8 @@ def test_config3_full_size_vs_oracle():
     m_gpu, m_ref, m0 = got["rho"].sum(), ref["rho"].sum(), rho.sum()
     record("config3_512_200", rho=e_rho, mass=abs(m_gpu - m_ref) / m_ref, drift_ref=abs(m_ref - m0) / m0,
            rho_span=float(ref["rho"].max() - ref["rho"].min()))
-    assert e_rho < 1e-5 and abs(m_gpu - m_ref) / m_ref < 1e-6
+    # measured rho 1.5e-7, mass 1.4e-12
+    assert e_rho < 1.5e-6 and abs(m_gpu - m_ref) / m_ref < 1.5e-11
 
 
 def test_adsorption_disk_image_vs_reference_code():
@@ -136,4 +141,4 @@ def test_adsorption_disk_image_vs_reference_code():
     e_ux = np.abs(c["ux"] - st["ux"]).max() / umax
     e_rho = np.abs(c["rho"] - st["rho"]).max() / np.abs(st["rho"]).max()
     record("adsorption_disk128_vs_reference_100", ux=e_ux, rho=e_rho)
-    assert e_ux < 1e-3 and e_rho < 1e-4
+    assert e_ux < 1e-5 and e_rho < 1.5e-5  # measured u_x 9.0e-7, rho 1.4e-6

@@ -42,7 +42,8 @@ def test_transport_gold_64(fixture64):
     e_uy = np.abs(px["uy"] - fixture64["transport_uy"]).max() / np.abs(fixture64["transport_ux"]).max()
     e_rho = np.abs(px["rho"] - fixture64["transport_rho"]).max() / 0.2355
     record("transport_gold_64", ux=e_ux, uy=e_uy, rho=e_rho)
-    assert e_ux < 1e-4 and e_uy < 1e-4 and e_rho < 1e-6
+    # measured on a GB300: u_x 4.0e-7, u_y 2.6e-7, rho 7.3e-13
+    assert e_ux < 4e-6 and e_uy < 3e-6 and e_rho < 1e-11
     assert s.launches > 0
 
 
@@ -57,7 +58,7 @@ def test_transport_residuals_and_break(fixture64):
     assert len(r) == 300
     e = np.abs(r - ref) / ref
     record("transport_residuals_64", max_rel=e.max(), median_rel=np.median(e))
-    assert np.median(e) < 1e-2
+    assert np.median(e) < 2e-5  # measured median 2.3e-6 (max 7.6e-5, late residuals ~1e-9)
     # break: tolerance just above the residual of step 250 in the oracle run
     tol = float(ref[249]) * 1.0001
     first = int(np.argmax(ref < tol)) + 1
@@ -83,7 +84,8 @@ def test_multiblock_matches_reference_code(case):
         e_rho = np.abs(c["rho"] - st[f"rho_{step}"]).max() / 0.2355
         e_f = np.abs(c["f"] - st[f"f_{step}"]).max() / 0.2355
         record(f"multiblock_{case}_{step}", ux=e_ux, rho=e_rho, f=e_f)
-        assert e_ux < 1e-4 and e_rho < 1e-6 and e_f < 1e-6
+        # measured (worst case and step): u_x 5.5e-7, rho 1.1e-12, f 4.7e-13
+        assert e_ux < 5e-6 and e_rho < 1e-11 and e_f < 5e-12
 
 
 def oracle_pair(pore, steps, multiblock=0, levels=2, dx=1e-9, kn=None, lp=None, edge_fine=0):
@@ -105,7 +107,7 @@ def test_multiblock_test_image_vs_oracle(fixture64):
     ref, got, s = oracle_pair(fixture64["pore"], 60, multiblock=1, kn=fixture64["kn"], lp=fixture64["locpore"])
     e = rel_err(got["ux"], ref["ux"])
     record("multiblock_testimage_vs_oracle", ux=e)
-    assert e < 1e-4
+    assert e < 3e-6  # measured 2.2e-7
 
 
 # The reference's multi-block scheme is not stable on every image: coarse cells
@@ -121,7 +123,8 @@ def test_disk_images_vs_oracle(n, levels, steps):
     e = rel_err(got["ux"], ref["ux"])
     e_rho = np.abs(got["rho"] - ref["rho"]).max() / 0.2355
     record(f"disks_{n}_L{levels}_vs_oracle", ux=e, rho=e_rho)
-    assert e < 1e-4 and e_rho < 1e-6
+    # measured: u_x 1.9e-7 / 1.2e-7 / 3.3e-7, rho 5.8e-9 / 8.7e-9 / 1.3e-7 (1, 2, 3 levels)
+    assert e < 3e-6 and e_rho < {1: 6e-8, 2: 9e-8, 3: 1.5e-6}[levels]
 
 
 def test_graph_path_matches_stepwise(fixture64):
@@ -189,7 +192,9 @@ def test_collision_and_wall_variants_vs_oracle(fixture64, collision, wall, multi
     e = rel_err(got["ux"], ref["ux"])
     e_f = np.abs(got["f"] - ref["f"]).max() / 0.2355
     record(f"variant_c{collision}_w{wall}_mb{multiblock}", ux=e, f=e_f)
-    assert e < 1e-4 and e_f < 1e-6
+    # measured: u_x <= 4.6e-7; f 2.1e-13 single block, 6.6e-8 on the multi-block
+    # test image (whose fine-buffer parents meet walls)
+    assert e < 5e-6 and e_f < (7e-7 if multiblock else 3e-12)
 
 
 VARIANTS_SB = [(2, 1), (1, 2), (0, 0), (1, 1), (0, 2), (0, 1)]
@@ -216,7 +221,8 @@ def test_variants_vs_reference_code(fixture64, collision, wall, multiblock):
     e_uy = np.abs(got["uy"] - st[f"{key}_uy"]).max() / np.abs(st[f"{key}_ux"]).max()
     e_f = np.abs(got["f"] - st[f"{key}_f"].reshape(-1, 9)).max() / 0.2355
     record(f"variant_ref_{key}", ux=e_ux, uy=e_uy, f=e_f)
-    assert e_ux < 1e-4 and e_uy < 1e-4 and e_f < 1e-6
+    # measured on a GB300: u_x <= 6.5e-7, u_y <= 4.6e-7, f <= 5.0e-13
+    assert e_ux < 7e-6 and e_uy < 5e-6 and e_f < 5e-12
 
 
 def test_plain_paths_agree_and_autotune():
@@ -281,7 +287,7 @@ def test_config2_full_size_vs_oracle():
     e_f = np.abs(got["f"].reshape(-1) - np.asarray(ref["f"]).reshape(-1)).max() / rho_in
     e_ux = rel_err(got["ux"], ref["ux"])
     record("config2_1024_vs_oracle_6", f=e_f, ux=e_ux)
-    assert e_f < 1e-6 and e_ux < 1e-4
+    assert e_f < 6e-7 and e_ux < 2e-6  # measured f 6.1e-8, u_x 1.7e-7
 
 
 def test_config1_permeability_vs_oracle():
@@ -305,7 +311,7 @@ def test_config1_permeability_vs_oracle():
     k_ref = ref["ux"].sum() / (n * n) * nu / p.fbody
     e = abs(k_gpu - k_ref) / abs(k_ref)
     record("config1_permeability_5000", rel=e, k=k_gpu)
-    assert e < 1e-5
+    assert e < 6e-6  # measured 5.6e-7; the target is 1e-5
 
 
 def test_disk_image_vs_reference_code():
@@ -319,4 +325,4 @@ def test_disk_image_vs_reference_code():
     e_ux = rel_err(c["ux"], st["ux"])
     e_rho = np.abs(c["rho"] - st["rho"]).max() / np.abs(st["rho"]).max()
     record("config1_disk_vs_reference_200", ux=e_ux, rho=e_rho)
-    assert e_ux < 1e-5 and e_rho < 1e-6
+    assert e_ux < 1.5e-6 and e_rho < 1e-7  # measured u_x 1.1e-7, rho 8.4e-9
