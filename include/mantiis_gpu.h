@@ -236,6 +236,16 @@ int mgpu_batch_advance(mgpu_batch *b, int n_steps);
 /* mgpu_observables of every image, 4 values per image */
 int mgpu_batch_observables(mgpu_batch *b, double *out);
 int mgpu_batch_set_stream(mgpu_batch *b, void *stream);
+/* How the batch steps: engine 0 = per-image phase launches on the concurrent
+ * streams above; engine 1 = one persistent launch per coarse step (two per
+ * graph replay) over every image, level, tile, wall record and interface row
+ * of the batch: blocks claim units of work in order and a stage of an image
+ * (a phase of its coarse step, an interface wave) starts when its previous
+ * stage is complete, as device-side counters show; `group` images (0 = all)
+ * are interleaved at a time.  Both engines give bit-identical states. */
+#define MGPU_ENGINE_STREAMS 0
+#define MGPU_ENGINE_PERSISTENT 1
+int mgpu_batch_set_engine(mgpu_batch *b, int engine, int group);
 int mgpu_batch_sync(mgpu_batch *b);
 int64_t mgpu_batch_launch_count(const mgpu_batch *b);
 int mgpu_batch_destroy(mgpu_batch *b);

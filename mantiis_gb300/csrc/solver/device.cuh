@@ -280,16 +280,22 @@ template <int P> __device__ __forceinline__ void load_raw(const LevelView &L, in
     }
 }
 
+// population load: through the read-only data path (NC: the slot is written by
+// no other thread during the launch) or an ordinary load (the persistent step,
+// where other blocks of the same launch wrote it in an earlier stage, which the
+// reading warp has acquired)
+template <bool NC> __device__ __forceinline__ float ldf(const float *p) { return NC ? __ldg(p) : *p; }
+
 // same reads through the read-only data path (the slots read by a thread are
-// written only by that thread in the same launch)
-template <int P>
+// written only by that thread in the same launch), or with NC = false through L2
+template <int P, bool NC = true>
 __device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, float raw[9], bool interior = false)
 {
     if (P == 0)
     {
         const int64_t s = site_of(L, x, y);
 #pragma unroll
-        for (int q = 0; q < 9; q++) raw[q] = __ldg(&L.f[q * L.plane + s]);
+        for (int q = 0; q < 9; q++) raw[q] = ldf<NC>(&L.f[q * L.plane + s]);
     }
     else if (interior)
     {
@@ -297,7 +303,7 @@ __device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, fl
         const int64_t s = site_of(L, x, y);
 #pragma unroll
         for (int q = 0; q < 9; q++)
-            raw[q] = __ldg(&L.f[d2q9::opp(q) * L.plane + s - d2q9::cy(q) * (int64_t)L.pitch - d2q9::cx(q)]);
+            raw[q] = ldf<NC>(&L.f[d2q9::opp(q) * L.plane + s - d2q9::cy(q) * (int64_t)L.pitch - d2q9::cx(q)]);
     }
     else
     {
@@ -305,7 +311,7 @@ __device__ __forceinline__ void load_raw_ro(const LevelView &L, int x, int y, fl
         for (int q = 0; q < 9; q++)
         {
             const int xs = wrapx(x - d2q9::cx(q), L.W), ys = wrapx(y - d2q9::cy(q), L.H);
-            raw[q] = __ldg(&L.f[d2q9::opp(q) * L.plane + site_of(L, xs, ys)]);
+            raw[q] = ldf<NC>(&L.f[d2q9::opp(q) * L.plane + site_of(L, xs, ys)]);
         }
     }
 }

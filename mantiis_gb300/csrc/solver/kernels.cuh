@@ -211,7 +211,7 @@ __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, 
 // finer level) are stepped here too, with the reads of special_cell for such a
 // record (interpolated values at the first substep, else the arrivals plus the
 // constant row), so the special-cell kernel keeps only the cells with walls.
-template <int P>
+template <int P, bool NC = true>
 __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C, const StepOpt &o, int t, int diff,
                                             int store_u, double &r_diff, double &r_norm)
 {
@@ -229,7 +229,7 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
     float om;
     if (!light)
     {
-        load_raw_ro<P>(L, x, y, df, interior);
+        load_raw_ro<P, NC>(L, x, y, df, interior);
         om = __ldg(&L.omega[s]);
     }
     else
@@ -245,7 +245,7 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
         else
         {
             // a direct state has parity 0: own slots, as load_raw<0>
-            load_raw_ro<P>(L, x, y, df, interior);
+            load_raw_ro<P, NC>(L, x, y, df, interior);
             if (!o.direct)
             {
                 const bool has_k = (flags & SF_HAS_K) != 0;
@@ -739,8 +739,8 @@ template <int P> __global__ void __launch_bounds__(128) k_ads_step_special(Level
 // velocity and populations in reference cell order, plus the residual terms
 // against the stored |u| and the pixel-area sums of u_x and rho.
 __global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int32_t *cell_level, const int32_t *cell_site,
-                                               int64_t n, double *rho_out, double *ux_out, double *uy_out, double *f_out,
-                                               int diff, int store_u, int red_slot)
+                                               const uint8_t *cell_buffer, int64_t n, double *rho_out, double *ux_out,
+                                               double *uy_out, double *f_out, int diff, int store_u, int red_slot)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double r_diff = 0.0, r_norm = 0.0, r_ux = 0.0, r_rho = 0.0;
@@ -791,8 +791,9 @@ __global__ void __launch_bounds__(256) k_cells(AllLevels A, Common C, const int3
         if (uy_out) uy_out[c] = vy;
         if (f_out)
             for (int q = 0; q < 9; q++) f_out[c * 9 + q] = d2q9::w(q) * (double)C.rho0 + (double)df[q];
-        const bool buffer = special && (((rec.m1 >> 17) & 0xFu) & SF_BUFFER);
-        if (!buffer)
+        // interface buffer cells cover pixels of finer cells: left out of the
+        // pixel-area sums (also those that step like plain cells)
+        if (!cell_buffer[c])
         {
             const double area = (double)(1 << (2 * l));
             r_ux = vx * area;
@@ -978,6 +979,194 @@ __global__ void __launch_bounds__(128) k_wave(const __grid_constant__ WaveLaunch
         const FineRowDev &row = d.fine[rr];
         if (d.pc) fine_child<1>(d.Lf, d.Lc, d.C, row, k, valid, d.pf);
         else fine_child<0>(d.Lf, d.Lc, d.C, row, k, valid, d.pf);
+    }
+}
+
+// ---- persistent step: one launch runs whole coarse steps of a group of
+// images.  The work is a list of units (one block of 256 threads each) in claim
+// order: 8 x tiles_per_warp tiles of 8x4 plain and light cells, 256 special
+// records with walls, or 64 interface rows.  Units are grouped in segments,
+// and the segments of one image form stages: the phases of its coarse step,
+// then its interface waves.  A stage starts only when the image's previous
+// stage is complete (the level substeps and the exchange that the phase engine
+// orders by stream order), which a block learns from that stage's completion
+// counter.  Blocks claim units with one atomic counter; every segment waits
+// only on units earlier in claim order, so the unit with the lowest unfinished
+// index can always run and the launch never deadlocks, whatever its grid size.
+// Stages of different images interleave in the claim order, so while one image
+// waits on its last units another image's work fills the GPU.
+struct PersistSeg
+{
+    int kind;        // 0 plain8 tiles, 1 special records, 2 coarse rows, 3 fine rows
+    int desc;        // StepDesc (kinds 0, 1) or PairDesc (2, 3) index
+    int unit0;       // first unit of the segment in claim order
+    int nunits;
+    int wait_ctr;    // counter that must reach wait_target first (-1: none)
+    unsigned wait_target;
+    int done_ctr;    // counter each finished unit increments
+    int pad;
+};
+
+constexpr int kPersistThreads = 256;
+constexpr int kPersistRecords = kPersistThreads; // special records per unit
+constexpr int kPersistRows = kPersistThreads / 4; // interface rows per unit (4 lanes each)
+constexpr unsigned kErrDepTimeout = 2u;
+// polls of a stage counter before a block gives up (an L2 round trip and a
+// 64 ns sleep each: about a second); a normal wait takes microseconds
+constexpr uint32_t kDepPolls = 1u << 22;
+
+struct PersistLaunch
+{
+    const PersistSeg *segs;
+    const StepDesc *sd;
+    const PairDesc *pd;
+    unsigned int *sync;   // [0] claim counter, [1 + c] stage counter c; zero at launch
+    unsigned int *err;    // device error word
+    int nseg, total_units;
+    int tiles_per_warp;   // 8x4 tiles each warp of a plain-cell unit steps
+};
+
+__device__ __forceinline__ bool wait_counter(const unsigned int *c, unsigned int target)
+{
+    for (uint32_t i = 0; i < kDepPolls; i++)
+    {
+        unsigned int v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(c) : "memory");
+        if (v >= target) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+// Stage-counter update with release semantics: after the block barrier, every
+// thread's stores of the unit are ordered before it (cumulativity).
+__device__ __forceinline__ void add_release(unsigned int *c, unsigned int v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(c), "r"(v) : "memory");
+}
+
+// The descriptor of a segment, staged in shared memory once per segment (the
+// array is read-only during the launch, so it takes the read-only path).
+template <typename T> __device__ __forceinline__ void stage_desc(T *dst, const T *src)
+{
+    static_assert(sizeof(T) % 4 == 0, "descriptor size");
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    for (int i = (int)threadIdx.x; i < (int)(sizeof(T) / 4); i += (int)blockDim.x) d[i] = __ldg(&s[i]);
+}
+
+// MINB: blocks per SM the register budget is sized for (more blocks, fewer
+// registers: the special-record and interface paths then spill a little; 5
+// blocks of 48 registers measured best).
+template <int MINB>
+__global__ void __launch_bounds__(kPersistThreads, MINB) k_step_persistent(const __grid_constant__ PersistLaunch P)
+{
+    __shared__ union
+    {
+        StepDesc sd;
+        PairDesc pd;
+    } s_desc;
+    __shared__ int s_unit, s_seg, s_next;
+    int seg_cache = 0;        // thread 0: segment of the last claim (claims only grow)
+    int ok_ctr = -1;          // thread 0: a counter already seen complete by this block
+    unsigned ok_target = 0u;
+    int staged = -1;          // segment whose descriptor is in shared memory
+    if (threadIdx.x == 0) s_next = (int)atomicAdd(P.sync, 1u);
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            const int u = s_next;
+            int seg = -1;
+            if (u < P.total_units)
+            {
+                while (seg_cache + 1 < P.nseg && __ldg(&P.segs[seg_cache + 1].unit0) <= u) seg_cache++;
+                seg = seg_cache;
+                const int wc = __ldg(&P.segs[seg].wait_ctr);
+                const unsigned wt = __ldg(&P.segs[seg].wait_target);
+                if (wc >= 0 && !(wc == ok_ctr && wt <= ok_target))
+                {
+                    if (wait_counter(P.sync + 1 + wc, wt))
+                    {
+                        ok_ctr = wc;
+                        ok_target = wt;
+                    }
+                    else
+                    {
+                        // an earlier unit never finished: stop (its waiters stop too)
+                        atomicOr(P.err, kErrDepTimeout);
+                        seg = -1;
+                    }
+                }
+                // the next claim is in flight while this unit runs
+                if (seg >= 0) s_next = (int)atomicAdd(P.sync, 1u);
+            }
+            s_unit = u;
+            s_seg = seg;
+        }
+        __syncthreads();
+        const int u = s_unit, seg = s_seg;
+        if (seg < 0) break;
+        const int kind = __ldg(&P.segs[seg].kind), desc = __ldg(&P.segs[seg].desc);
+        const int k = u - __ldg(&P.segs[seg].unit0);
+        if (seg != staged)
+        {
+            if (kind < 2) stage_desc(&s_desc.sd, &P.sd[desc]);
+            else stage_desc(&s_desc.pd, &P.pd[desc]);
+            staged = seg;
+            __syncthreads();
+        }
+        double r_diff = 0.0, r_norm = 0.0;
+        if (kind == 0)
+        {
+            const StepDesc &d = s_desc.sd;
+            const int t0 = (k * 8 + (int)(threadIdx.x >> 5)) * P.tiles_per_warp;
+#pragma unroll 1
+            for (int j = 0; j < P.tiles_per_warp; j++)
+            {
+                const int t = t0 + j;
+                if (t < d.L.ntiles8)
+                {
+                    if (d.o.parity) plain_tile8<1, false>(d.L, d.C, d.o, t, 0, 0, r_diff, r_norm);
+                    else plain_tile8<0, false>(d.L, d.C, d.o, t, 0, 0, r_diff, r_norm);
+                }
+            }
+        }
+        else if (kind == 1)
+        {
+            const StepDesc &d = s_desc.sd;
+            const int i = k * kPersistRecords + (int)threadIdx.x;
+            if (i < d.spec_count)
+            {
+                if (d.o.parity) special_cell<1>(d.L, d.C, d.o, d.spec_begin + i, 0, 0, r_diff, r_norm);
+                else special_cell<0>(d.L, d.C, d.o, d.spec_begin + i, 0, 0, r_diff, r_norm);
+            }
+        }
+        else
+        {
+            // 4 lanes per row, as k_wave
+            const PairDesc &d = s_desc.pd;
+            const int v = k * kPersistThreads + (int)threadIdx.x;
+            const int r = v >> 2, c = v & 3;
+            const bool valid = r < d.nrows;
+            const int rr = valid ? r : 0;
+            if (kind == 2)
+            {
+                const CoarseRowDev &row = d.coarse[rr];
+                if (d.pf) coarse_row<1>(d.Lf, d.Lc, d.C, row, c, valid, d.pc);
+                else coarse_row<0>(d.Lf, d.Lc, d.C, row, c, valid, d.pc);
+            }
+            else
+            {
+                const FineRowDev &row = d.fine[rr];
+                if (d.pc) fine_child<1>(d.Lf, d.Lc, d.C, row, c, valid, d.pf);
+                else fine_child<0>(d.Lf, d.Lc, d.C, row, c, valid, d.pf);
+            }
+        }
+        // the unit's stores, then its count (release): a waiter's acquire load
+        // of the counter then sees them
+        __syncthreads();
+        if (threadIdx.x == 0) add_release(P.sync + 1 + __ldg(&P.segs[seg].done_ctr), 1u);
     }
 }
 

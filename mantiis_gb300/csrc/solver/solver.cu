@@ -150,6 +150,18 @@ struct PhasePlan
     std::map<std::string, PhaseVariant> variants;
 };
 
+// Work list of the persistent step (dev::k_step_persistent) for a state of the
+// level parities: segments in claim order and the descriptors they point to.
+struct PersistPlan
+{
+    DevBuf<dev::PersistSeg> segs;
+    DevBuf<dev::StepDesc> sd;
+    DevBuf<dev::PairDesc> pd;
+    int nseg = 0, total_units = 0, nctr = 0;
+    int tiles_per_warp = 1;
+    int64_t bytes = 0;
+};
+
 } // namespace
 
 // Streams that run beside a context's (or a batch's) main stream within a
@@ -232,6 +244,7 @@ struct mgpu_ctx
     DevBuf<SpecialRec> specials;
     DevBuf<float> ktab, side, ibuf;
     DevBuf<int32_t> cell_level, cell_site;
+    DevBuf<uint8_t> cell_buffer; // 1 for interface buffer cells (Grid2D::gridIsBuffer)
     DevBuf<double> red;     // kRing * 4
     double *red_host = nullptr; // pinned staging copy of the accumulators
     DevBuf<double> out_rho, out_ux, out_uy, out_f;
@@ -573,8 +586,9 @@ void cells_pass(mgpu_ctx *ctx, double *rho, double *ux, double *uy, double *f, b
     int64_t n = ctx->grid.n_cells;
     if (n == 0) return;
     dim3 grid((unsigned)((n + 255) / 256)), block(256);
-    dev::k_cells<<<grid, block, 0, st ? st : ctx->stream>>>(ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p, n, rho,
-                                                   ux, uy, f, diff ? 1 : 0, store_u ? 1 : 0, red_slot);
+    dev::k_cells<<<grid, block, 0, st ? st : ctx->stream>>>(ctx->all(), ctx->common(), ctx->cell_level.p, ctx->cell_site.p,
+                                                            ctx->cell_buffer.p, n, rho, ux, uy, f, diff ? 1 : 0,
+                                                            store_u ? 1 : 0, red_slot);
     launch_check(ctx);
 }
 
@@ -1112,6 +1126,190 @@ void phase_step(PhasePlan &P, const std::vector<mgpu_ctx *> &ctxs, cudaStream_t 
     }
 }
 
+// ---- persistent step, host side.  The work of `ncoarse` coarse steps of the
+// images `ctxs`, from the state `ahead` coarse steps on, as one list of units
+// for dev::k_step_persistent.  Per image the stages are its phases (the 8x4
+// tiles of every level stepping in the phase, with the light special records,
+// and the records with walls) and then its interface waves, exactly the work
+// and order of phase_step on one image; images are interleaved stage by stage
+// in groups of `group` images (0: all), so that the images in flight at once
+// can be kept to what shares the L2.
+void build_persist(PersistPlan &PP, const std::vector<mgpu_ctx *> &ctxs, int ahead, int ncoarse, int group,
+                   int tiles_per_warp, cudaStream_t st)
+{
+    struct Item
+    {
+        int kind, desc, units;
+    };
+    using Stage = std::vector<Item>;
+    std::vector<std::vector<Stage>> stages(ctxs.size());
+    std::vector<dev::StepDesc> sd;
+    std::vector<dev::PairDesc> pd;
+    auto units_of = [](int64_t n, int per) { return (int)((n + per - 1) / per); };
+    for (size_t i = 0; i < ctxs.size(); i++)
+    {
+        const mgpu_ctx *c = ctxs[i];
+        const PhasePlan &P = *c->plan;
+        for (int a = 0; a < ncoarse; a++)
+        {
+            const int ah = ahead + a;
+            auto steps_of = [&](int l) { return c->lv[l].steps + (int64_t)ah * c->lay.levels[l].substeps; };
+            for (int ph = 0; ph < P.nphase; ph++)
+            {
+                Stage stg;
+                for (const int4 &e : P.entries[ph])
+                {
+                    const int l = e.y, k = e.z;
+                    const LevelLayout &ll = c->lay.levels[l];
+                    const int64_t stp = steps_of(l) + e.w;
+                    const bool mb = c->grid.multiblock;
+                    dev::StepDesc d;
+                    std::memset(&d, 0, sizeof(d));
+                    d.L = c->view(l);
+                    d.C = c->common();
+                    d.o.parity = (int)(stp & 1);
+                    d.o.direct = stp == 0 ? 1 : 0;
+                    d.o.first_sub = k == 0 ? 1 : 0;
+                    d.o.snap_store = (mb && k == 0) ? 1 : 0;
+                    d.o.snap_use = (mb && k > 0) ? 1 : 0;
+                    d.spec_begin = ll.spec_begin;
+                    d.spec_count = (int)ll.spec_heavy; // the light records are stepped with the tiles
+                    if (!ll.tile8_list.empty())
+                    {
+                        sd.push_back(d);
+                        stg.push_back({0, (int)sd.size() - 1, units_of((int64_t)ll.tile8_list.size(), 8 * tiles_per_warp)});
+                    }
+                    if (ll.spec_heavy > 0)
+                    {
+                        sd.push_back(d);
+                        stg.push_back({1, (int)sd.size() - 1, units_of(ll.spec_heavy, dev::kPersistRecords)});
+                    }
+                }
+                if (!stg.empty()) stages[i].push_back(stg);
+            }
+            // interface waves: wave w = coarse rows of pair (w+1, w+2), fine rows of pair (w, w+1)
+            for (int w = 0; w < P.nwave; w++)
+            {
+                Stage stg;
+                for (const int2 &pr : P.pairs)
+                {
+                    const InterfaceDev &it = c->itf[pr.y];
+                    const int lf = it.l1 - 1, lc = it.l1;
+                    dev::PairDesc d;
+                    std::memset(&d, 0, sizeof(d));
+                    d.Lf = c->view(lf);
+                    d.Lc = c->view(lc);
+                    d.C = c->common();
+                    d.coarse = it.coarse.p;
+                    d.fine = it.fine.p;
+                    d.pf = (int)((steps_of(lf) + c->lay.levels[lf].substeps) & 1);
+                    d.pc = (int)((steps_of(lc) + c->lay.levels[lc].substeps) & 1);
+                    if (it.ncoarse && it.l1 - 1 == w)
+                    {
+                        d.kind = 0;
+                        d.nrows = it.ncoarse;
+                        pd.push_back(d);
+                        stg.push_back({2, (int)pd.size() - 1, units_of(it.ncoarse, dev::kPersistRows)});
+                    }
+                    if (it.nfine && it.l1 == w)
+                    {
+                        d.kind = 1;
+                        d.nrows = it.nfine;
+                        pd.push_back(d);
+                        stg.push_back({3, (int)pd.size() - 1, units_of(it.nfine, dev::kPersistRows)});
+                    }
+                }
+                if (!stg.empty()) stages[i].push_back(stg);
+            }
+        }
+    }
+    // claim order: groups of images one after another; within a group stage s
+    // of every image before stage s + 1 of any
+    std::vector<dev::PersistSeg> segs;
+    std::vector<std::vector<int>> ctr(ctxs.size());
+    std::vector<std::vector<unsigned>> stage_units(ctxs.size());
+    int nctr = 0;
+    for (size_t i = 0; i < ctxs.size(); i++)
+        for (const Stage &stg : stages[i])
+        {
+            ctr[i].push_back(nctr++);
+            unsigned u = 0;
+            for (const Item &it : stg) u += (unsigned)it.units;
+            stage_units[i].push_back(u);
+        }
+    const size_t G = group > 0 ? (size_t)group : ctxs.size();
+    int unit = 0;
+    for (size_t g0 = 0; g0 < ctxs.size(); g0 += G)
+    {
+        const size_t g1 = std::min(ctxs.size(), g0 + G);
+        size_t smax = 0;
+        for (size_t i = g0; i < g1; i++) smax = std::max(smax, stages[i].size());
+        for (size_t sidx = 0; sidx < smax; sidx++)
+            for (size_t i = g0; i < g1; i++)
+            {
+                if (sidx >= stages[i].size()) continue;
+                for (const Item &it : stages[i][sidx])
+                {
+                    dev::PersistSeg sg{};
+                    sg.kind = it.kind;
+                    sg.desc = it.desc;
+                    sg.unit0 = unit;
+                    sg.nunits = it.units;
+                    sg.wait_ctr = sidx > 0 ? ctr[i][sidx - 1] : -1;
+                    sg.wait_target = sidx > 0 ? stage_units[i][sidx - 1] : 0u;
+                    sg.done_ctr = ctr[i][sidx];
+                    segs.push_back(sg);
+                    unit += it.units;
+                }
+            }
+    }
+    PP.bytes = 0;
+    PP.segs.upload(segs, PP.bytes, st);
+    PP.sd.upload(sd, PP.bytes, st);
+    PP.pd.upload(pd, PP.bytes, st);
+    PP.nseg = (int)segs.size();
+    PP.total_units = unit;
+    PP.nctr = nctr;
+    PP.tiles_per_warp = tiles_per_warp;
+}
+
+// the persistent kernel's register budget is sized for this many blocks per SM
+constexpr int kPersistMinBlocks = 5;
+
+// blocks of a persistent launch: as many as fit on the GPU at once
+int persist_grid(int sm_count, int total_units)
+{
+    static int per_sm = 0;
+    if (!per_sm)
+    {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::k_step_persistent<kPersistMinBlocks>,
+                                                         dev::kPersistThreads, 0));
+        per_sm = std::max(per_sm, 1);
+    }
+    return std::max(1, std::min(total_units, sm_count * per_sm));
+}
+
+// Enqueues one persistent launch of the plan (its counters zeroed first).
+void launch_persist(const PersistPlan &PP, unsigned int *sync, unsigned int *err, int sm_count, cudaStream_t st,
+                    int64_t &launches)
+{
+    if (PP.total_units == 0) return;
+    CK(cudaMemsetAsync(sync, 0, (size_t)(1 + PP.nctr) * sizeof(unsigned int), st));
+    dev::PersistLaunch L{};
+    L.segs = PP.segs.p;
+    L.sd = PP.sd.p;
+    L.pd = PP.pd.p;
+    L.sync = sync;
+    L.err = err;
+    L.nseg = PP.nseg;
+    L.total_units = PP.total_units;
+    L.tiles_per_warp = PP.tiles_per_warp;
+    dev::k_step_persistent<kPersistMinBlocks>
+        <<<(unsigned)persist_grid(sm_count, PP.total_units), dev::kPersistThreads, 0, st>>>(L);
+    CK(cudaGetLastError());
+    launches++;
+}
+
 // plain_path -1: times the three plain-cell paths (0 direct 32x8 tiles, 1 TMA
 // pipeline for x-interior 32x8 tiles, 2 direct 8x4 warp tiles) over a few
 // coarse steps from the initial state, puts the state back after each and
@@ -1317,6 +1515,11 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     ctx->ibuf.zero(s);
     ctx->cell_level.upload(ctx->lay.cell_level, acct, s);
     ctx->cell_site.upload(ctx->lay.cell_site, acct, s);
+    {
+        const std::vector<uint8_t> buf(ctx->grid.is_buffer.begin(), ctx->grid.is_buffer.end());
+        ctx->cell_buffer.upload(buf, acct, s);
+        CK(cudaStreamSynchronize(s)); // buf goes out of scope
+    }
     ctx->red.alloc((size_t)(kRing + 2) * 4, acct); // the ring and two scratch slots
     ctx->red.zero(s);
     ctx->errword.alloc(1, acct);
@@ -2062,6 +2265,18 @@ struct mgpu_batch
     cudaGraphExec_t graph = nullptr;
     std::string graph_key;
     int64_t graph_launches = 0, launches = 0;
+    // engine 1: every coarse step (two inside the graph) is one persistent
+    // launch over all images (dev::k_step_persistent), images interleaved in
+    // groups of `group` (0: all); engine 0: per-image phase launches on the
+    // concurrent streams above
+    // 8x4 tiles per warp of a plain-cell unit of the persistent kernel (config-2
+    // batch of 4 at 5 blocks per SM: 4 -> 408 us per coarse step, 2 -> 443, 1 -> 459;
+    // at 4 blocks per SM 436, at 3 630)
+    int engine = 0, group = 0, tiles_per_warp = 4;
+    std::map<std::string, std::unique_ptr<PersistPlan>> pplans;
+    DevBuf<unsigned int> sync; // claim and stage counters of the persistent launch
+    int64_t bytes = 0;
+    int sm_count = 1;
 };
 
 namespace
@@ -2084,12 +2299,41 @@ void batch_leave(mgpu_batch *b)
         if (c->stream != b->stream) CK(cudaStreamWaitEvent(c->stream, b->ev_done, 0));
 }
 
+// the persistent plan of the batch's current state for n coarse steps
+PersistPlan &batch_persist_plan(mgpu_batch *b, int n)
+{
+    const std::string key = state_key(b->ctxs, 0) + "/" + std::to_string(n);
+    auto it = b->pplans.find(key);
+    if (it != b->pplans.end()) return *it->second;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(b->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) throw std::logic_error("persistent plan missing during graph capture");
+    std::unique_ptr<PersistPlan> PP(new PersistPlan());
+    build_persist(*PP, b->ctxs, 0, n, b->group, b->tiles_per_warp, b->stream);
+    if ((size_t)(1 + PP->nctr) > b->sync.n) throw std::logic_error("persistent plan: too many stage counters");
+    b->bytes += PP->bytes;
+    return *b->pplans.emplace(key, std::move(PP)).first->second;
+}
+
 // n coarse steps of every image: each image on its own stream with its own
 // phase launches, so that one image's small launches (interface waves, the
-// sparse coarse levels) overlap another's; images share no data
+// sparse coarse levels) overlap another's; images share no data.  With the
+// persistent engine: one launch for the n steps of all images.
 void batch_step(mgpu_batch *b, int n = 1)
 {
     const dev::PhaseArgs none{0, 0, 0};
+    if (b->engine == 1)
+    {
+        PersistPlan &PP = batch_persist_plan(b, n);
+        launch_persist(PP, b->sync.p, b->ctxs[0]->errword.p, b->sm_count, b->stream, b->launches);
+        for (auto *c : b->ctxs)
+        {
+            for (size_t l = 0; l < c->lv.size(); l++) c->lv[l].steps += (int64_t)n * c->lay.levels[l].substeps;
+            c->coarse_done += n;
+            c->ref_t += n;
+        }
+        return;
+    }
     if (b->img_stream.empty())
     {
         for (int k = 0; k < n; k++) phase_step(*b->plan, b->ctxs, b->stream, b->lanes, none, b->launches);
@@ -2163,6 +2407,10 @@ int mgpu_batch_create(mgpu_ctx *const *ctxs, int n, mgpu_batch **out)
         }
         b->ctx_ev.resize(b->ctxs.size());
         for (auto &e : b->ctx_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->sm_count = b->ctxs[0]->sm_count;
+        // stage counters of two coarse steps: at most 2^(L-1) phases and L waves
+        // per image and step (L <= 4)
+        b->sync.alloc(1 + b->ctxs.size() * 2 * (8 + 4), b->bytes);
         *out = b.release();
         return MGPU_OK;
     });
@@ -2191,6 +2439,7 @@ int mgpu_batch_advance(mgpu_batch *b, int n_steps)
         if (left >= 2 && !b->graph)
         {
             // two coarse steps: every level of every image returns to its parity
+            if (b->engine == 1) batch_persist_plan(b, 2);
             plan_variant(*b->plan, b->ctxs, 0);
             plan_variant(*b->plan, b->ctxs, 1);
             for (auto *c : b->ctxs)
@@ -2319,6 +2568,26 @@ int mgpu_batch_sync(mgpu_batch *b)
     return guarded(nullptr, [&]() {
         if (!b) throw std::invalid_argument("null batch");
         CK(cudaStreamSynchronize(b->stream));
+        for (auto *c : b->ctxs) check_device_error(c);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_engine(mgpu_batch *b, int engine, int group)
+{
+    return guarded(nullptr, [&]() {
+        if (!b || engine < 0 || engine > 1 || group < 0) throw std::invalid_argument("bad argument");
+        if (engine == b->engine && group == b->group) return MGPU_OK;
+        CK(cudaStreamSynchronize(b->stream));
+        if (b->graph)
+        {
+            CK(cudaGraphExecDestroy(b->graph));
+            b->graph = nullptr;
+        }
+        b->graph_key.clear();
+        if (group != b->group) b->pplans.clear();
+        b->engine = engine;
+        b->group = group;
         return MGPU_OK;
     });
 }

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mgpu_batch_advance": (C.c_int, [P, C.c_int]),
     "mgpu_batch_observables": (C.c_int, [P, F64P]),
     "mgpu_batch_set_stream": (C.c_int, [P, P]),
+    "mgpu_batch_set_engine": (C.c_int, [P, C.c_int, C.c_int]),
     "mgpu_batch_sync": (C.c_int, [P]),
     "mgpu_batch_launch_count": (C.c_int64, [P]),
     "mgpu_batch_destroy": (C.c_int, [P]),
@@ -464,6 +465,12 @@ class Batch:
 
     def set_stream(self, stream_handle):
         self._check(lib().mgpu_batch_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def set_engine(self, engine, group=0):
+        """engine 0: per-image phase launches on concurrent streams; 1: one
+        persistent launch per coarse step over all images (mgpu_batch_set_engine),
+        interleaving `group` images at a time (0 = all)."""
+        self._check(lib().mgpu_batch_set_engine(self._h, int(engine), int(group)))
 
     def sync(self):
         self._check(lib().mgpu_batch_sync(self._h))

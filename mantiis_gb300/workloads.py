@@ -3,6 +3,7 @@ benchmark configurations (the reference ships no benchmark images).
 
 config1: 128x128, disk radii U[4,10], porosity 0.65, Kn ~0.1, single block
 config2: 1024x1024, disk radii U[6,40], porosity U[0.5,0.7], Kn U[0.01,1], 3 levels
+config2_steady: the config-2 generator with 2 levels, void x edges, Kn U[0.01,0.02]
 config3: 512x512, porosity 0.6 (Shan-Chen adsorption)
 config4: side in {128,...,2048}, porosity U[0.45,0.75], 1-3 levels, log-uniform Kn in [0.01, 2]
 
@@ -16,8 +17,8 @@ import numpy as np
 from .native import generate_disks, pore_properties, units
 
 
-def image(n, rmin, rmax, porosity, kn_mean, seed):
-    pore = generate_disks(n, rmin, rmax, porosity, seed)
+def image(n, rmin, rmax, porosity, kn_mean, seed, open_x_edges=False):
+    pore = generate_disks(n, rmin, rmax, porosity, seed, open_x_edges=open_x_edges)
     H, kn_unit = pore_properties(pore, 1.0, 1.0)  # kn_unit = 1 / H
     mfp = units()["mfp"]
     void = pore == 1
@@ -35,6 +36,24 @@ def config2(index=0):
     phi = rng.uniform(0.5, 0.7)
     kn = rng.uniform(0.01, 1.0)
     return image(1024, 6, 40, phi, kn, 2000 + index)
+
+
+def config2_steady(index=0):
+    """A config-2 image on which the reference's multi-block scheme reaches a
+    steady state: the same generator (1024x1024, disk radii U[6,40], porosity
+    U[0.5,0.7]) with two quadtree levels (the reference's own depth limit),
+    the two columns at either x edge void (solid pixels on the x-periodic seam
+    leak mass under the wall-then-periodic order) and Kn U[0.01,0.02].  At
+    these disk sizes tau_s - 1/2 ~ mfp / dx grows with Kn: from a mean tau_s of
+    about 1.6 (Kn 0.028) the coarse/fine exchange slowly amplifies a mode and the
+    run diverges after ~20k steps, above ~1.8 (Kn 0.035) within a few thousand;
+    three levels diverge at 1024^2 for any Kn."""
+    rng = np.random.default_rng(2500 + index)
+    phi = rng.uniform(0.5, 0.7)
+    kn = rng.uniform(0.01, 0.02)
+    d = image(1024, 6, 40, phi, kn, 2500 + index, open_x_edges=True)
+    d["levels"] = 2
+    return d
 
 
 def config3(index=0):

@@ -148,8 +148,12 @@ def test_deterministic(fixture64):
     assert np.array_equal(runs[0], runs[1])
 
 
-def test_batch_matches_single_contexts(fixture64):
-    # a batch of images with 1, 2 and 3 levels steps each exactly like its own context
+@pytest.mark.parametrize("engine,group", [(0, 0), (1, 0), (1, 2)])
+def test_batch_matches_single_contexts(fixture64, engine, group):
+    # a batch of images with 1, 2 and 3 levels steps each exactly like its own
+    # context: per-image launches on concurrent streams (engine 0) and the
+    # persistent launch over all images (engine 1, images interleaved all at
+    # once or two at a time)
     from mantiis_gb300 import Batch
 
     imgs = [(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=1e-9))]
@@ -163,6 +167,7 @@ def test_batch_matches_single_contexts(fixture64):
     for s in solo:
         s.advance(9)
     b = Batch(grouped)
+    b.set_engine(engine, group)
     b.advance(4)   # the first step from the initial state, then a graph of two, then one
     b.advance(5)
     b.sync()
