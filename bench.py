@@ -177,6 +177,53 @@ STEADY_WORKLOAD = ("config2_steady: 1024x1024 seeded disk images (r U[6,40], por
                    "2-level quadtree, Kn U[0.01,0.02]")
 
 
+STEADY_BATCH_WORKLOAD = ("config4_steady: seeded disk images of side {128..2048} (r n/256..n/32, porosity "
+                         "U[0.45,0.75], void x edges), 1-2 levels, log-uniform Kn in [0.01, 0.12] single block, "
+                         "Kn U[0.01,0.02] x min(1024/n, 2) with two levels; all images in one batch")
+
+
+def steady_batch_leg(count, stream, chunk=1000, tol=1e-6, max_steps=100000):
+    """The config-4 set in its steady variant: `count` images of uneven size and
+    depth stepped together as one batch until every image's permeability
+    changes by less than `tol` (relative) over `chunk` steps; settled images
+    keep stepping with the rest.  GPU time with CUDA events around the run."""
+    import torch
+
+    from mantiis_gb300 import Batch, Solver, default_params, workloads
+    from mantiis_gb300.surrogate import run_batch_to_steady
+
+    imgs = [workloads.config4_steady(i) for i in range(count)]
+    sol = []
+    for img in imgs:
+        mb = img["levels"] > 1
+        p = default_params(multiblock=int(mb), max_allowed_level=max(2, img["levels"]), dx=img["dx"],
+                           edge_fine=int(mb), concurrent=1)
+        s = Solver(img["pore"], img["kn"], img["locpore"], p)
+        s.set_stream(stream.cuda_stream)
+        sol.append(s)
+    b = Batch(sol)
+    b.set_stream(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    steps, k = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    done = int(steps.max())
+    lu = float(sum(s.info["lu_per_step"] for s in sol))
+    out = {"workload": STEADY_BATCH_WORKLOAD, "images": count,
+           "criterion": f"relative permeability change below {tol:g} over {chunk} steps",
+           "settled": int((steps < max_steps).sum()), "coarse_steps": done, "gpu_seconds": ms / 1e3,
+           "mlups": lu * done / (ms / 1e3) / 1e6, "lu_per_step": lu,
+           "sides": [int(im["pore"].shape[0]) for im in imgs], "levels": [int(im["levels"]) for im in imgs],
+           "steps_to_settle": [int(v) for v in steps], "permeability": [float(v) for v in k],
+           "positive": bool((np.asarray(k) > 0).all()), "finite": bool(np.isfinite(k).all())}
+    b.close()
+    for s in sol:
+        s.close()
+    return out
+
+
 def steady_state_leg(count, stream, chunk=500, tol=1e-6, max_steps=200000):
     """Images on which the reference's multi-block scheme has a steady state,
     each run from rest until its permeability changes by less than `tol`
@@ -346,6 +393,8 @@ def main():
                     help="repeat the timed K-step window until the windows cover this much time")
     ap.add_argument("--steady-images", type=int, default=4,
                     help="images of the steady-state leg (0 = skip it)")
+    ap.add_argument("--steady-batch", type=int, default=0,
+                    help="also run this many config4_steady images to steady state as one batch")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--properties", type=int, default=0, metavar="N")
     ap.add_argument("--adsorption", action="store_true", help="time the config-3 adsorption step instead")
@@ -502,6 +551,9 @@ def main():
     steady = None
     if rank == 0 and args.steady_images > 0:
         steady = steady_state_leg(args.steady_images, stream)
+    steady_batch = None
+    if rank == 0 and args.steady_batch > 0:
+        steady_batch = steady_batch_leg(args.steady_batch, stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -538,6 +590,7 @@ def main():
             "timing": {"windows": len(windows), "window_steps": K, "ms_min": min(windows), "ms_max": max(windows),
                        "seconds_timed": total_ms / 1e3},
             "steady_state": steady,
+            **({"steady_batch": steady_batch} if steady_batch else {}),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,
                     "steps": Ke, "seconds": e2e_s},

@@ -6,6 +6,7 @@ config2: 1024x1024, disk radii U[6,40], porosity U[0.5,0.7], Kn U[0.01,1], 3 lev
 config2_steady: the config-2 generator with 2 levels, void x edges, Kn U[0.01,0.02]
 config3: 512x512, porosity 0.6 (Shan-Chen adsorption)
 config4: side in {128,...,2048}, porosity U[0.45,0.75], 1-3 levels, log-uniform Kn in [0.01, 2]
+config4_steady: config 4 with void x edges, 1-2 levels, Kn kept where the reference's scheme settles
 
 Local pore size H comes from the reference's skeleton rule; the lattice
 spacing dx is then chosen so that the mean Knudsen number over the void
@@ -53,6 +54,28 @@ def config2_steady(index=0):
     kn = rng.uniform(0.01, 0.02)
     d = image(1024, 6, 40, phi, kn, 2500 + index, open_x_edges=True)
     d["levels"] = 2
+    return d
+
+
+def config4_steady(index=0):
+    """A config-4 image on which the reference's scheme reaches a steady state:
+    side in {128, ..., 2048}, disk radii n/256..n/32, porosity U[0.45, 0.75],
+    the two columns at either x edge void, one or two quadtree levels.  Kn is
+    kept where the reference's scheme settles: single block log-uniform in
+    [0.01, 0.12], two levels U[0.01, 0.02] x min(1024 / n, 2) (the relaxation
+    times of config2_steady).  At larger Kn the FP64 oracle itself finds no
+    steady state on such images: a 128^2 single-block image at Kn 1.48 loses
+    0.7 % of its mass per 1000 steps and its mean flow runs against the force."""
+    rng = np.random.default_rng(4500 + index)
+    n = int(rng.choice([128, 256, 512, 1024, 2048]))
+    phi = rng.uniform(0.45, 0.75)
+    levels = int(rng.integers(1, 3))
+    if levels == 1:
+        kn = float(np.exp(rng.uniform(np.log(0.01), np.log(0.12))))
+    else:
+        kn = float(rng.uniform(0.01, 0.02) * min(1024 / n, 2.0))
+    d = image(n, max(2, n // 256), max(4, n // 32), phi, kn, 4500 + index, open_x_edges=True)
+    d["levels"] = levels
     return d
 
 

@@ -1,0 +1,99 @@
+"""Long runs against the FP64 oracle: the 1024x1024 two-level multi-block
+image run to steady state (its permeability and fields), and the config-3
+Shan-Chen workload for its full 20000 steps (the adsorbed-layer density
+profile and the total mass).  The oracle's runs take tens of minutes on the
+host, so they are committed fixtures (tests/golden/make_steady.py,
+tests/golden/make_config3.py); the GPU runs take seconds."""
+import sys
+
+import numpy as np
+import pytest
+from conftest import GOLDEN, load
+
+from mantiis_gb300 import HostGrid, Solver, default_params, generate_disks, workloads
+from test_gpu_transport import record
+
+sys.path.insert(0, str(GOLDEN))
+import make_config3  # noqa: E402
+import make_steady  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def test_permeability_observable_multiblock():
+    # mgpu_observables' k is the pixel mean of u_x (a cell once per covered
+    # pixel, interface buffer cells not at all) times nu over F_body, the same
+    # formula the fixtures use on the oracle's cells
+    pore = generate_disks(256, 6, 30, 0.6, 77, open_x_edges=True)
+    kn = np.where(pore == 1, 0.015, 0.0)
+    lp = np.where(pore == 1, 7.73, 0.0)
+    p = default_params(multiblock=1, edge_fine=1, tol=0.0)
+    g = HostGrid(pore, kn, lp, p)
+    s = Solver(pore, kn, lp, p)
+    s.advance(50)
+    k_obs = s.observables()["permeability"]
+    k_cells = make_steady.permeability(g, s.cells()["ux"], p.fbody)
+    assert g.cells["is_buffer"].sum() > 0
+    assert abs(k_obs - k_cells) <= 1e-9 * abs(k_cells)
+
+
+def test_steady_multiblock_1024_vs_fp64():
+    # workloads.config2_steady(0): 1024x1024 seeded disks, two levels, void x
+    # edges, Kn 0.0145.  The GPU runs to the oracle's criterion (relative
+    # change of k below 1e-8 over 1000 steps); permeability and fields are
+    # compared with the FP64 oracle's steady state
+    st = load("steady_mb1024.npz")
+    img = workloads.config2_steady(0)
+    assert abs(img["dx"] - float(st["dx"])) <= 1e-12 * img["dx"]
+    p = default_params(multiblock=1, max_allowed_level=img["levels"], dx=img["dx"], edge_fine=1, tol=0.0)
+    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    assert s.n_cells == int(st["n_cells"])
+    hist, steps = [], 0
+    chunk = int(st["chunk"])
+    while steps < 2 * int(st["steps"]):
+        s.advance_graph(chunk)
+        steps += chunk
+        hist.append(s.observables()["permeability"])
+        if len(hist) >= 3 and abs(hist[-1] - hist[-3]) < 1e-8 * abs(hist[-1]):
+            break
+    c = s.cells()
+    k_gpu = make_steady.permeability(g, c["ux"], p.fbody)
+    k_ref = float(st["k"])
+    e_k = abs(k_gpu - k_ref) / abs(k_ref)
+    sub = st["cells"]
+    umax = np.abs(st["ux"]).max()
+    e_ux = np.abs(c["ux"][sub] - st["ux"]).max() / umax
+    e_uy = np.abs(c["uy"][sub] - st["uy"]).max() / umax
+    e_rho = np.abs(c["rho"][sub] - st["rho"]).max() / np.abs(st["rho"]).max()
+    bmax = np.abs(st["ux_blocks"]).max()
+    e_blocks = np.abs(make_steady.block_means(g, c["ux"]) - st["ux_blocks"]).max() / bmax
+    record("steady_mb1024", k=e_k, ux=e_ux, uy=e_uy, rho=e_rho, ux_blocks=e_blocks, steps=steps,
+           oracle_steps=int(st["steps"]))
+    assert abs(hist[-1] - k_gpu) <= 1e-9 * abs(k_gpu)  # the observable is the same k
+    assert e_k < 1e-5
+    assert e_ux < 1e-4 and e_uy < 1e-4 and e_rho < 1e-6 and e_blocks < 1e-5
+
+
+def test_config3_20000_vs_fp64():
+    # config 3 for its Nt = 20000 steps: the adsorbed-layer density profile
+    # (mean density at wall distance 1..12) and the total mass against the FP64
+    # oracle's run
+    st = load("config3_20000.npz")
+    img, p, g, rho0 = make_config3.setup()
+    s = Solver(img["pore"], img["kn"], img["locpore"], p)
+    s.set_equilibrium(rho0, np.zeros_like(rho0), np.zeros_like(rho0))
+    mass = [rho0.sum()]
+    for _ in range(int(st["steps"]) // 1000):
+        s.advance(1000)
+        mass.append(s.cells()["rho"].sum())
+    c = s.cells()
+    prof = make_config3.profile(g, c["rho"], make_config3.wall_distance(img["pore"]))
+    ref = st["profile"]
+    span = ref.max() - ref.min()
+    e_prof = np.abs(prof - ref).max() / span
+    e_mass = np.abs(np.array(mass) - st["mass"]).max() / st["mass"][0]
+    e_rho = np.abs(c["rho"][st["cells"]] - st["rho"]).max() / np.abs(st["rho"]).max()
+    record("config3_20000", profile=e_prof, mass=e_mass, rho=e_rho, profile_span=span,
+           drift_ref=abs(st["mass"][-1] - st["mass"][0]) / st["mass"][0])
+    assert e_prof < 1e-4 and e_mass < 1e-9 and e_rho < 1e-5
