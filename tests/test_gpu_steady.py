@@ -20,6 +20,13 @@ import make_steady  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
+def fixture(name):
+    # the oracle's long runs are generated once (tests/golden/make_*.py)
+    if not (GOLDEN / name).exists():
+        pytest.skip(f"{name} not generated")
+    return load(name)
+
+
 def test_permeability_observable_multiblock():
     # mgpu_observables' k is the pixel mean of u_x (a cell once per covered
     # pixel, interface buffer cells not at all) times nu over F_body, the same
@@ -42,7 +49,7 @@ def test_steady_multiblock_1024_vs_fp64():
     # edges, Kn 0.0145.  The GPU runs to the oracle's criterion (relative
     # change of k below 1e-8 over 1000 steps); permeability and fields are
     # compared with the FP64 oracle's steady state
-    st = load("steady_mb1024.npz")
+    st = fixture("steady_mb1024.npz")
     img = workloads.config2_steady(0)
     assert abs(img["dx"] - float(st["dx"])) <= 1e-12 * img["dx"]
     p = default_params(multiblock=1, max_allowed_level=img["levels"], dx=img["dx"], edge_fine=1, tol=0.0)
@@ -79,7 +86,7 @@ def test_config3_20000_vs_fp64():
     # config 3 for its Nt = 20000 steps: the adsorbed-layer density profile
     # (mean density at wall distance 1..12) and the total mass against the FP64
     # oracle's run
-    st = load("config3_20000.npz")
+    st = fixture("config3_20000.npz")
     img, p, g, rho0 = make_config3.setup()
     s = Solver(img["pore"], img["kn"], img["locpore"], p)
     s.set_equilibrium(rho0, np.zeros_like(rho0), np.zeros_like(rho0))
