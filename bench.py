@@ -13,9 +13,20 @@ A bench step is one coarse time step of every image of the batch.
             reference's per-step residual and break test (mgpu_run), and the
             per-cell fields are read back (mgpu_download_cells)
   roofline  the finest-level step kernel: 72 B per lattice update (9 FP32
-            populations read + 9 written) over its CUDA-event launch time
+            populations read + 9 written) over its CUDA-event launch time;
+            batch_achieved / batch_frac: the same 72 B per update at the
+            batch's own rate (value)
+  timing    the K-step window is timed repeatedly until the windows cover
+            --min-seconds (at least 3); value is the median window
+  steady_state  config2_steady images (1024^2, two levels, on which the
+            reference's scheme has a steady state), each run from rest to a
+            relative permeability change below 1e-6 over 1000 steps: steps,
+            GPU seconds, permeability
+  steady_batch  (--steady-batch N) N config4_steady images as one batch to
+            the same criterion
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference's step)
-            on the host cores, on a bounded sample of the same workload
+            on the host cores, on a bounded sample of the same workload, with
+            all threads and with one
 
 --impl reference times that CPU implementation alone, as the reference arm.
 --properties N times the pore-property pipeline (skeleton, distance transforms,
@@ -393,6 +404,8 @@ def main():
                     help="repeat the timed K-step window until the windows cover this much time")
     ap.add_argument("--steady-images", type=int, default=4,
                     help="images of the steady-state leg (0 = skip it)")
+    ap.add_argument("--engine", type=int, default=0, choices=[0, 1],
+                    help="batch engine: 0 per-image launches on concurrent streams, 1 one persistent launch per step")
     ap.add_argument("--steady-batch", type=int, default=0,
                     help="also run this many config4_steady images to steady state as one batch")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
@@ -447,6 +460,7 @@ def main():
     # coarse steps per CUDA graph (captured during the warm-up)
     batch = Batch(solvers)
     batch.set_stream(stream.cuda_stream)
+    batch.set_engine(args.engine, 0)
     warm = args.warmup + (args.warmup % 2)
     batch.advance(warm)
     torch.cuda.synchronize()
@@ -576,7 +590,9 @@ def main():
                        "levels": [int(im["levels"]) for im in imgs] if args.workload == "config4" else imgs[0]["levels"],
                        "lu_per_step_per_gpu": lu_step, "device_state_mb_per_gpu": round(state_mb, 1),
                        "l2": "inputs larger than L2 (state of the batch > 129 MB)",
-                       "graph": "one CUDA graph of 2 coarse steps for the whole batch, images on L2-sized concurrent streams",
+                       "graph": ("one CUDA graph of 2 coarse steps for the whole batch, images on L2-sized concurrent "
+                                 "streams" if args.engine == 0 else
+                                 "one CUDA graph of 2 coarse steps for the whole batch, one persistent launch per step"),
                        "state_finite_after_timed_steps": finite,
                        **({} if finite else {"state_note": "the reference's multi-block scheme diverges on these "
                                                            "images (its FP64 restatement too); the step's work "

@@ -476,6 +476,226 @@ def evaluate(net, n, count, seed0=90000, chunk=500, tol=1e-6, max_steps=200000, 
     return out
 
 
+# ---- config 5: the network trained on the config-4 set's steady fields and
+# used on held-out 1024^2 multi-block images
+
+
+def solver_params(d, **kw):
+    """Parameters of a workloads image dict (single block or 'levels' quadtree levels)."""
+    from .native import default_params
+
+    levels = int(d.get("levels", 1))
+    mb = levels > 1
+    return default_params(multiblock=int(mb), max_allowed_level=max(2, levels), dx=d["dx"], edge_fine=int(mb), **kw)
+
+
+def steady_samples(images, chunk=1000, tol=1e-6, max_steps=100000, log=None):
+    """Runs the images (workloads dicts) to steady state as one batch and
+    returns (input, target, mask) of those that settled with a positive
+    permeability (images of mixed sizes: a list, not an array)."""
+    from .native import Batch, Solver
+
+    sol = [Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, concurrent=1)) for d in images]
+    b = Batch(sol)
+    t0 = time.perf_counter()
+    steps, k = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
+    out = []
+    for d, s, st, kk in zip(images, sol, steps, k):
+        if st < max_steps and np.isfinite(kk) and kk > 0:
+            out.append((network_input(d["pore"], d["kn"]), steady_targets(s), (d["pore"] == 1).astype(np.float32)))
+    if log:
+        log(f"data: {len(images)} images to steady state in {int(steps.max())} steps "
+            f"({time.perf_counter() - t0:.1f} s), kept {len(out)}")
+    b.close()
+    for s in sol:
+        s.close()
+    return out
+
+
+def train_mixed(net, samples, epochs=60, lr=1e-3, pixels_per_batch=8 * 128 * 128, seed=0, log=None):
+    """Adam on the masked squared error over samples of mixed sizes: each step
+    takes equal-size samples adding up to about pixels_per_batch pixels.
+    Returns the mean loss of each epoch."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    by_size = {}
+    for x, y, m in samples:
+        by_size.setdefault(x.shape[-1], []).append((x, encode(y[None], net.scale)[0], m))
+    groups = {n: tuple(torch.tensor(np.stack([v[i] for v in vs]), device="cuda") for i in range(3))
+              for n, vs in by_size.items()}
+    history = []
+    t0 = time.perf_counter()
+    for ep in range(epochs):
+        batches = []
+        for n, (X, Y, M) in groups.items():
+            per = max(1, pixels_per_batch // (n * n))
+            order = rng.permutation(len(X))
+            batches += [(n, order[i:i + per]) for i in range(0, len(order), per)]
+        rng.shuffle(batches)
+        tot, cnt = 0.0, 0
+        for n, idx in batches:
+            X, Y, M = groups[n]
+            sel = torch.tensor(idx, device="cuda")
+            x, y, m = X[sel].contiguous(), Y[sel].contiguous(), M[sel].contiguous()
+            net.zero_grad()
+            p = net.forward(x, keep=True)
+            loss, dp = masked_loss(p, y, m)
+            net.backward(dp)
+            net.adam(lr)
+            tot += float(loss.item()) * len(idx)
+            cnt += len(idx)
+        history.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep + 1}: loss {history[-1]:.4e} ({time.perf_counter() - t0:.1f} s)")
+    return history
+
+
+def smooth_noise(n, seed, passes=8):
+    """n x n random field of unit RMS, correlated over a few pixels (neighbour
+    averages on the torus)."""
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal((n, n))
+    for _ in range(passes):
+        f = (f + np.roll(f, 1, 0) + np.roll(f, -1, 0) + np.roll(f, 1, 1) + np.roll(f, -1, 1)) / 5.0
+    return f / np.sqrt((f * f).mean())
+
+
+def warm_start_study(net, images, errors=(0.3, 0.1, 0.03, 0.01), blocks=(8, 32, 128), chunk=1000, tol=1e-6,
+                     max_steps=200000, log=None):
+    """Per held-out image: steps and GPU seconds to the permeability criterion
+    (relative change below tol over chunk steps) from rest (cold), from the
+    network's prediction (warm: velocity only, and velocity with density), and
+    from the converged cold state itself, in parts and with errors put back:
+    the exact velocity and density ('exact'), the velocity alone at the rest
+    density ('velocity_exact'), the density alone at rest ('density_exact'),
+    the exact velocity with the density deviation off by a relative e
+    ('density_amplitude_e': (1 + e) drho; 'density_local_e': (1 + e xi) drho, xi
+    a smooth unit-RMS random field) or averaged over B x B pixel blocks
+    ('density_blocks_B'), and the velocity off by 30 % with the exact density.
+    These rows tell which part of a prediction sets the saving and how accurate
+    it has to be.  net may be None (the rows without the network)."""
+    from .native import Solver
+
+    out = []
+    for i, d in enumerate(images):
+        p = solver_params(d)
+        n = int(d["pore"].shape[0])
+        row = {"n": n, "levels": int(d.get("levels", 1)), "kn_mean": d.get("kn_mean")}
+        cold = Solver(d["pore"], d["kn"], d["locpore"], p)
+        sc, tc, kc = run_to_steady(cold, chunk, tol, max_steps)
+        row.update(cold_steps=int(sc), cold_s=tc, k=kc)
+        steady = cold.cells()
+        px = cold.pixels()
+        cx, cy, _ = cold.cell_positions()
+        rho_in = cold.info["rho_in"]
+        tgt = steady_targets(cold)
+        cold.close()
+        rest = np.full(steady["ux"].shape, rho_in)
+        zero = np.zeros_like(rest)
+        drho = steady["rho"] - rho_in
+
+        def restart(rho, ux, uy):
+            sv = Solver(d["pore"], d["kn"], d["locpore"], p)
+            sv.set_equilibrium(rho, ux, uy)
+            st, ts, ks = run_to_steady(sv, chunk, tol, max_steps)
+            sv.close()
+            return int(st)
+
+        if net is not None:
+            for name, dens in (("warm", False), ("warm_density", True)):
+                w = Solver(d["pore"], d["kn"], d["locpore"], p)
+                t0 = time.perf_counter()
+                warm_start(w, net, d["pore"], d["kn"], use_density=dens)
+                t_pred = time.perf_counter() - t0
+                sw, tw, kw = run_to_steady(w, chunk, tol, max_steps)
+                w.close()
+                row.update({f"{name}_steps": int(sw), f"{name}_s": tw + t_pred, f"{name}_k_rel": abs(kw - kc) / abs(kc)})
+            pred = predict(net, d["pore"], d["kn"])
+            void = d["pore"] == 1
+            for c, name in ((0, "ux"), (2, "drho")):
+                row[f"prediction_rel_err_{name}"] = float(np.abs(pred[c] - tgt[c])[void].mean()
+                                                          / max(np.abs(tgt[c])[void].mean(), 1e-30))
+        row["exact_steps"] = restart(steady["rho"], steady["ux"], steady["uy"])
+        row["velocity_exact_steps"] = restart(rest, steady["ux"], steady["uy"])
+        row["density_exact_steps"] = restart(steady["rho"], zero, zero)
+        row["velocity_0.3_density_exact_steps"] = restart(steady["rho"], 1.3 * steady["ux"], 1.3 * steady["uy"])
+        xi = smooth_noise(n, 7000 + i)[cy, cx]
+        for e in errors:
+            row[f"density_amplitude_{e:g}_steps"] = restart(rho_in + (1 + e) * drho, steady["ux"], steady["uy"])
+            row[f"density_local_{e:g}_steps"] = restart(rho_in + (1 + e * xi) * drho, steady["ux"], steady["uy"])
+        void = px["rho"] != 0
+        for B in blocks:
+            if n % B:
+                continue
+            # pixel-area mean of the density deviation over B x B blocks (fluid pixels)
+            dpx = np.where(void, px["rho"] - rho_in, 0.0)
+            num = dpx.reshape(n // B, B, n // B, B).sum(axis=(1, 3))
+            den = void.reshape(n // B, B, n // B, B).sum(axis=(1, 3))
+            blk = np.where(den > 0, num / np.maximum(den, 1), 0.0)
+            coarse = np.kron(blk, np.ones((B, B)))[cy, cx]
+            row[f"density_blocks_{B}_steps"] = restart(rho_in + coarse, steady["ux"], steady["uy"])
+        # the column and row means of the exact density deviation, and the
+        # column model of darcy_column_density
+        dpx = np.where(void, px["rho"] - rho_in, 0.0)
+        cnt_c = np.maximum(void.sum(axis=0), 1)
+        cnt_r = np.maximum(void.sum(axis=1), 1)
+        col = np.broadcast_to(dpx.sum(axis=0) / cnt_c, (n, n))[cy, cx]
+        rowm = np.broadcast_to((dpx.sum(axis=1) / cnt_r)[:, None], (n, n))[cy, cx]
+        row["density_columns_steps"] = restart(rho_in + col, steady["ux"], steady["uy"])
+        row["density_rows_steps"] = restart(rho_in + rowm, steady["ux"], steady["uy"])
+        model = darcy_column_density(d["pore"], d["locpore"], cold_fbody(p))[cy, cx]
+        row["density_column_model_steps"] = restart(rho_in + model, steady["ux"], steady["uy"])
+        row["density_column_model_rest_velocity_steps"] = restart(rho_in + model, zero, zero)
+        row["column_model_rel_err"] = float(np.abs(model - col).max() / max(np.abs(col).max(), 1e-30))
+        out.append(row)
+        if log:
+            log(str(row))
+    return out
+
+
+def cold_fbody(p):
+    return float(p.fbody)
+
+
+def darcy_column_density(pore, locpore, fbody):
+    """Density deviation of a Darcy model of the x-periodic pore image, one value
+    per column: each column conducts C(x) = sum over its void pixels of H^2
+    (H the local pore size, Poiseuille's law), the flux Q is the same through
+    every column, so the pressure gradient is dp/dx = F - Q / C(x) with Q set
+    by periodicity (the gradients add up to zero over the period); rho - rho_in
+    = 3 p (c_s^2 = 1/3), zero mean over the void pixels.  Returns n x n."""
+    n = pore.shape[0]
+    void = pore == 1
+    C = np.where(void, np.asarray(locpore, np.float64) ** 2, 0.0).sum(axis=0)
+    inv = np.where(C > 0, 1.0 / np.maximum(C, 1e-300), 0.0)
+    g = fbody * (1.0 - inv / inv.mean())   # dp/dx per column, zero mean
+    p = np.cumsum(g) - 0.5 * g             # pressure at the column centres
+    drho = 3.0 * np.broadcast_to(p, (n, n))
+    drho = drho - drho[void].mean()
+    return np.where(void, drho, 0.0)
+
+
+def config5(train_images=64, eval_images=4, epochs=60, lr=1e-3, log=None):
+    """Trains the network on the steady fields of workloads.config4_steady
+    images (sides 128-2048, 1-2 levels) and runs warm_start_study on the
+    held-out 1024^2 two-level images workloads.config2_steady(0..eval-1)."""
+    from . import workloads
+
+    samples = steady_samples([workloads.config4_steady(i) for i in range(train_images)], log=log)
+    net = UNet(seed=5)
+    ys = [y for _, y, _ in samples]
+    ms = [m for _, _, m in samples]
+    net.scale = np.array([np.median(np.concatenate([np.abs(y[c][m > 0]) for y, m in zip(ys, ms)])) + 1e-30
+                          for c in range(3)])
+    t0 = time.perf_counter()
+    hist = train_mixed(net, samples, epochs=epochs, lr=lr, log=log)
+    t_train = time.perf_counter() - t0
+    res = warm_start_study(net, [workloads.config2_steady(i) for i in range(eval_images)], log=log)
+    return dict(train_images=len(samples), epochs=epochs, train_seconds=t_train, final_loss=hist[-1],
+                first_loss=hist[0], cases=res)
+
+
 def main(argv=None):
     """python -m mantiis_gb300.surrogate --size 128 --train 512 --epochs 300 --eval 8
     Trains the network on solver-generated steady fields and prints a JSON
@@ -489,8 +709,20 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--eval", type=int, default=8)
     ap.add_argument("--lr", type=float, default=5e-4)
+    ap.add_argument("--config5", action="store_true",
+                    help="train on the config-4 steady set, study the warm start on 1024^2 images")
+    ap.add_argument("--study-only", action="store_true",
+                    help="the warm-start study on the 1024^2 images without training a network")
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)  # noqa: E731
+    if a.study_only:
+        from . import workloads
+
+        print(json.dumps(warm_start_study(None, [workloads.config2_steady(i) for i in range(a.eval)], log=log)))
+        return
+    if a.config5:
+        print(json.dumps(config5(train_images=a.train, eval_images=a.eval, epochs=a.epochs, lr=a.lr, log=log)))
+        return
     X, Y, M = make_dataset(a.size, a.train, log=log)
     net = UNet(seed=1)
     net.scale = target_scale(Y, M)

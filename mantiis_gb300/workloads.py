@@ -74,7 +74,14 @@ def config4_steady(index=0):
         kn = float(np.exp(rng.uniform(np.log(0.01), np.log(0.12))))
     else:
         kn = float(rng.uniform(0.01, 0.02) * min(1024 / n, 2.0))
-    d = image(n, max(2, n // 256), max(4, n // 32), phi, kn, 4500 + index, open_x_edges=True)
+    # the generator's fill of pixels with untabulated neighbourhoods can put
+    # solid pixels back into the void x-edge columns; such a pixel has wall and
+    # x-periodic links at once, where the reference's order loses mass, so
+    # those images are drawn again with another seed
+    for attempt in range(400):
+        d = image(n, max(2, n // 256), max(4, n // 32), phi, kn, 4500 + index + 100000 * attempt, open_x_edges=True)
+        if d["pore"][1:-1][:, [0, 1, n - 2, n - 1]].all():
+            break
     d["levels"] = levels
     return d
 
