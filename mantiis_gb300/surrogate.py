@@ -648,6 +648,21 @@ def warm_start_study(net, images, errors=(0.3, 0.1, 0.03, 0.01), blocks=(8, 32, 
         row["density_column_model_steps"] = restart(rho_in + model, steady["ux"], steady["uy"])
         row["density_column_model_rest_velocity_steps"] = restart(rho_in + model, zero, zero)
         row["column_model_rel_err"] = float(np.abs(model - col).max() / max(np.abs(col).max(), 1e-30))
+        # Darcy block models: mobility from the local pore size (H^2), and from the
+        # converged velocity (|u| per pixel)
+        H = np.asarray(d["locpore"], np.float64)
+        speed = np.hypot(px["ux"], px["uy"])
+        for B in (16, 32, 64):
+            if n % B:
+                continue
+            for name, mob in (("geometry", H * H), ("speed", speed)):
+                dm = darcy_block_density(d["pore"], mob, cold_fbody(p), B)
+                row[f"darcy_{name}_{B}_steps"] = restart(rho_in + dm[cy, cx], steady["ux"], steady["uy"])
+                blk = dpx.reshape(n // B, B, n // B, B).sum(axis=(1, 3)) / np.maximum(
+                    void.reshape(n // B, B, n // B, B).sum(axis=(1, 3)), 1)
+                row[f"darcy_{name}_{B}_rel_err"] = float(
+                    np.abs(np.where(void, dm - np.kron(blk, np.ones((B, B))), 0.0)).max()
+                    / max(np.abs(blk).max(), 1e-30))
         out.append(row)
         if log:
             log(str(row))
@@ -656,6 +671,57 @@ def warm_start_study(net, images, errors=(0.3, 0.1, 0.03, 0.01), blocks=(8, 32, 
 
 def cold_fbody(p):
     return float(p.fbody)
+
+
+def darcy_block_density(pore, mobility, fbody, block=32):
+    """Density deviation of a Darcy model of the x-periodic image on blocks of
+    block x block pixels: block mobility K_b = the mean of `mobility` over the
+    block's pixels (solid pixels count 0); between neighbouring blocks the flux
+    is T (F B - dp) across x faces (periodic) and -T dp across y faces (none
+    through the top and bottom), T the harmonic mean of the two mobilities;
+    every block conserves mass.  The scale of the mobility cancels, only its
+    variation sets the pressure.  rho - rho_in = 3 p (c_s^2 = 1/3), piecewise
+    constant on the blocks, zero mean over the void pixels.  Returns n x n."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.linalg import spsolve
+
+    n = pore.shape[0]
+    m = n // block
+    void = pore == 1
+    mob = np.where(void, np.asarray(mobility, np.float64), 0.0)
+    K = mob.reshape(m, block, m, block).mean(axis=(1, 3))
+    K = np.maximum(K, 1e-12 * max(K.max(), 1e-300))
+    idx = np.arange(m * m).reshape(m, m)  # [row (y), column (x)]
+    rows, cols, vals = [], [], []
+    rhs = np.zeros(m * m)
+
+    def face(i, j, T, drive):
+        # flux from block i to block j: T (drive - (p_j - p_i)); mass balance of both
+        rows.extend([i, i, j, j])
+        cols.extend([i, j, j, i])
+        vals.extend([T, -T, T, -T])
+        rhs[i] -= T * drive
+        rhs[j] += T * drive
+
+    for y in range(m):
+        for x in range(m):
+            xr = (x + 1) % m
+            Tx = 2 * K[y, x] * K[y, xr] / (K[y, x] + K[y, xr])
+            face(idx[y, x], idx[y, xr], Tx, fbody * block)
+            if y + 1 < m:
+                Ty = 2 * K[y, x] * K[y + 1, x] / (K[y, x] + K[y + 1, x])
+                face(idx[y, x], idx[y + 1, x], Ty, 0.0)
+    # A p = rhs (flux out minus in); the pressure is fixed up to a constant:
+    # pin block 0 and shift afterwards
+    A = coo_matrix((vals, (rows, cols)), shape=(m * m, m * m)).tocsr()
+    A = A.tolil()
+    A[0, :] = 0
+    A[0, 0] = 1.0
+    rhs[0] = 0.0
+    p = spsolve(A.tocsr(), rhs).reshape(m, m)
+    drho = 3.0 * np.kron(p, np.ones((block, block)))
+    drho = drho - drho[void].mean()
+    return np.where(void, drho, 0.0)
 
 
 def darcy_column_density(pore, locpore, fbody):

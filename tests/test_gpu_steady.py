@@ -78,8 +78,11 @@ def test_steady_multiblock_1024_vs_fp64():
     record("steady_mb1024", k=e_k, ux=e_ux, uy=e_uy, rho=e_rho, ux_blocks=e_blocks, steps=steps,
            oracle_steps=int(st["steps"]))
     assert abs(hist[-1] - k_gpu) <= 1e-9 * abs(k_gpu)  # the observable is the same k
+    # measured on a GB300 (32.5k GPU steps against the oracle's 25.5k to the same
+    # criterion): k 4.5e-6, u_x 5.3e-6, u_y 2.9e-6 of max|u_x|, rho 1.7e-8, 8x8-block
+    # means of u_x 5.2e-6; the target for k is 1e-5
     assert e_k < 1e-5
-    assert e_ux < 1e-4 and e_uy < 1e-4 and e_rho < 1e-6 and e_blocks < 1e-5
+    assert e_ux < 1e-5 and e_uy < 1e-5 and e_rho < 2e-7 and e_blocks < 1e-5
 
 
 def test_config3_20000_vs_fp64():

@@ -67,7 +67,10 @@ def test_adam_step_and_bf16_copy():
 def test_train_and_warm_start_small():
     # the whole loop on a small case: solver-made training data, training on
     # the GPU kernels, then the warm-started solver converges to the cold
-    # start's permeability; the step counts of both are recorded
+    # start's permeability; the step counts of both are recorded.  The network
+    # predicts the velocity well enough to look right but saves no steps (on
+    # one of these images it costs 1000 more): the slow part of the convergence
+    # is the density field (test_warm_start_needs_the_density)
     from mantiis_gb300 import surrogate as S
     from test_gpu_transport import record
 
@@ -84,3 +87,41 @@ def test_train_and_warm_start_small():
         assert r["permeability_rel_diff"] < 1e-5
         record(f"warm_start_64_{i}", cold_steps=r["cold_steps"], warm_steps=r["warm_steps"],
                prediction_rel_err=r["prediction_rel_err"], k_rel=r["permeability_rel_diff"])
+
+
+def test_warm_start_needs_the_density():
+    # What a warm start has to get right: restarting from the converged state
+    # itself reaches the criterion in far fewer steps than the cold start, but
+    # the converged velocity alone, at the rest density, saves nothing -- the
+    # slow part of the convergence is the density (pressure) field
+    from mantiis_gb300 import Solver
+    from mantiis_gb300 import surrogate as S
+    from test_gpu_transport import record
+
+    from mantiis_gb300 import workloads
+
+    # a 1024^2 two-level image whose cold start is slow (117k steps)
+    d = workloads.config2_steady(3)
+    p = S.solver_params(d)
+    chunk, tol = 1000, 1e-6
+    cold = Solver(d["pore"], d["kn"], d["locpore"], p)
+    sc, _, kc = S.run_to_steady(cold, chunk, tol, 200000)
+    st = cold.cells()
+    rho_in = cold.info["rho_in"]
+    cold.close()
+
+    def restart(rho, ux, uy):
+        s = Solver(d["pore"], d["kn"], d["locpore"], p)
+        s.set_equilibrium(rho, ux, uy)
+        n, _, k = S.run_to_steady(s, chunk, tol, 200000)
+        s.close()
+        assert abs(k - kc) < 1e-5 * abs(kc)
+        return n
+
+    exact = restart(st["rho"], st["ux"], st["uy"])
+    velocity_only = restart(np.full_like(st["rho"], rho_in), st["ux"], st["uy"])
+    record("warm_start_needs_density_1024", cold_steps=sc, exact_steps=exact, velocity_only_steps=velocity_only)
+    # measured on a GB300: cold 117000, exact 6000, velocity only 117000
+    assert sc < 200000
+    assert exact <= 0.2 * sc
+    assert velocity_only >= 0.9 * sc
