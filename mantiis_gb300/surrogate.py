@@ -742,6 +742,138 @@ def darcy_column_density(pore, locpore, fbody):
     return np.where(void, drho, 0.0)
 
 
+# ---- the coarse density field: the part of the steady state that sets the
+# convergence (warm_start_study).  A second network of the same kind works on
+# the image coarsened to blocks of COARSE x COARSE pixels, so that its deepest
+# features span most of the domain, and predicts the block means of the density
+# deviation in units of 3 F n (the pressure a force F builds over the domain).
+
+COARSE = 8
+
+
+def coarse_input(pore, kn, block=COARSE):
+    """2 x n/B x n/B: block porosity and the block mean of log10(Kn) / 2 over void pixels."""
+    n = pore.shape[0]
+    m = n // block
+    void = (pore == 1)
+    cnt = void.reshape(m, block, m, block).sum(axis=(1, 3))
+    lk = np.where(void, np.log10(np.maximum(kn, 1e-12)) / 2.0, 0.0).reshape(m, block, m, block).sum(axis=(1, 3))
+    return np.stack([cnt / float(block * block), np.where(cnt > 0, lk / np.maximum(cnt, 1), 0.0)]).astype(np.float32)
+
+
+def coarse_density(solver, pore, block=COARSE):
+    """1 x n/B x n/B target: block means of rho - rho_in over void pixels, over 3 F n."""
+    px = solver.pixels()
+    n = pore.shape[0]
+    m = n // block
+    void = pore == 1
+    d = np.where(void, px["rho"] - solver.info["rho_in"], 0.0).reshape(m, block, m, block).sum(axis=(1, 3))
+    cnt = void.reshape(m, block, m, block).sum(axis=(1, 3))
+    blk = np.where(cnt > 0, d / np.maximum(cnt, 1), 0.0)
+    return (blk / (3.0 * solver.params.fbody * n))[None].astype(np.float32)
+
+
+def coarse_samples(images, chunk=1000, tol=1e-6, max_steps=100000, log=None):
+    """(coarse input, coarse density target, block mask) of the images that
+    settle with a positive permeability, all stepped as one batch."""
+    from .native import Batch, Solver
+
+    sol = [Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, concurrent=1)) for d in images]
+    b = Batch(sol)
+    t0 = time.perf_counter()
+    steps, k = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
+    out = []
+    for d, s, st, kk in zip(images, sol, steps, k):
+        if st < max_steps and np.isfinite(kk) and kk > 0:
+            x = coarse_input(d["pore"], d["kn"])
+            out.append((x, coarse_density(s, d["pore"]), (x[0] > 0).astype(np.float32)))
+    if log:
+        log(f"coarse data: {len(images)} images in {int(steps.max())} steps ({time.perf_counter() - t0:.1f} s), "
+            f"kept {len(out)}")
+    b.close()
+    for s in sol:
+        s.close()
+    return out
+
+
+def augment(samples, rng):
+    """x-periodic shifts and y mirror images (symmetries of the flow problem)."""
+    out = []
+    for x, y, m in samples:
+        sh = int(rng.integers(0, x.shape[-1]))
+        x, y, m = (np.roll(a, sh, axis=-1) for a in (x, y, m))
+        if rng.random() < 0.5:
+            x, y, m = x[..., ::-1, :], y[..., ::-1, :], m[..., ::-1, :]
+        out.append((np.ascontiguousarray(x), np.ascontiguousarray(y), np.ascontiguousarray(m)))
+    return out
+
+
+def train_coarse(samples, epochs=400, lr=1e-3, widths=(32, 64, 64, 128, 128), seed=0, log=None):
+    """The coarse network on augmented samples (a fresh shift and mirror every epoch)."""
+    net = UNet(widths=widths, cin=2, cout=1, seed=seed)
+    ys = np.concatenate([np.abs(y[0][m > 0]) for _, y, m in samples])
+    net.scale = np.array([np.median(ys) + 1e-30])
+    rng = np.random.default_rng(seed)
+    hist = []
+    t0 = time.perf_counter()
+    for ep in range(epochs):
+        h = train_mixed(net, augment(samples, rng), epochs=1, lr=lr, pixels_per_batch=8 * 64 * 64, seed=ep)
+        hist.append(h[0])
+        if log and (ep + 1) % 50 == 0:
+            log(f"coarse epoch {ep + 1}: loss {hist[-1]:.4e} ({time.perf_counter() - t0:.1f} s)")
+    return net, hist
+
+
+def predict_coarse_density(net, pore, kn, fbody, block=COARSE):
+    """n x n density deviation from the coarse network: its block values times
+    3 F n, zero mean over the void pixels, 0 on solid pixels."""
+    import torch
+
+    n = pore.shape[0]
+    x = torch.tensor(coarse_input(pore, kn, block)[None], dtype=torch.float32, device="cuda")
+    y = net.forward(x).cpu().numpy()[0, 0].astype(np.float64)
+    blk = np.sinh(y) * net.scale[0] * 3.0 * fbody * n
+    void = pore == 1
+    d = np.kron(blk, np.ones((block, block)))
+    d = d - d[void].mean()
+    return np.where(void, d, 0.0)
+
+
+def coarse_study(net, images, chunk=1000, tol=1e-6, max_steps=200000, log=None):
+    """Cold start against the coarse network's density (velocity at rest) on
+    each image; also the error of the predicted block densities."""
+    from .native import Solver
+
+    out = []
+    for d in images:
+        p = solver_params(d)
+        n = d["pore"].shape[0]
+        cold = Solver(d["pore"], d["kn"], d["locpore"], p)
+        sc, tc, kc = run_to_steady(cold, chunk, tol, max_steps)
+        tgt = coarse_density(cold, d["pore"])[0] * 3.0 * p.fbody * n
+        cx, cy, _ = cold.cell_positions()
+        rho_in = cold.info["rho_in"]
+        cold.close()
+        pred = predict_coarse_density(net, d["pore"], d["kn"], p.fbody)
+        pb = pred.reshape(n // COARSE, COARSE, n // COARSE, COARSE)[:, 0, :, 0]
+        mask = coarse_input(d["pore"], d["kn"])[0] > 0
+        tb = tgt - tgt[mask].mean()
+        err = float(np.abs(pb - tb)[mask].mean() / max(np.abs(tb)[mask].mean(), 1e-30))
+        w = Solver(d["pore"], d["kn"], d["locpore"], p)
+        t0 = time.perf_counter()
+        rho = rho_in + predict_coarse_density(net, d["pore"], d["kn"], p.fbody)[cy, cx]
+        w.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
+        t_pred = time.perf_counter() - t0
+        sw, tw, kw = run_to_steady(w, chunk, tol, max_steps)
+        w.close()
+        row = dict(n=int(n), kn_mean=d.get("kn_mean"), cold_steps=int(sc), cold_s=tc, warm_steps=int(sw),
+                   warm_s=tw + t_pred, k_rel=abs(kw - kc) / abs(kc), block_density_rel_err=err)
+        out.append(row)
+        if log:
+            log(str(row))
+    return out
+
+
 def config5(train_images=64, eval_images=4, epochs=60, lr=1e-3, log=None):
     """Trains the network on the steady fields of workloads.config4_steady
     images (sides 128-2048, 1-2 levels) and runs warm_start_study on the
@@ -777,10 +909,22 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=5e-4)
     ap.add_argument("--config5", action="store_true",
                     help="train on the config-4 steady set, study the warm start on 1024^2 images")
+    ap.add_argument("--coarse", action="store_true",
+                    help="train the coarse density network and warm-start the 1024^2 images with its density")
     ap.add_argument("--study-only", action="store_true",
                     help="the warm-start study on the 1024^2 images without training a network")
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)  # noqa: E731
+    if a.coarse:
+        from . import workloads
+
+        samples = coarse_samples([workloads.config4_steady(i) for i in range(a.train)]
+                                 + [dict(workloads.config2_steady(i)) for i in range(8, 8 + a.train // 2)], log=log)
+        net, hist = train_coarse(samples, epochs=a.epochs, lr=a.lr, log=log)
+        res = coarse_study(net, [workloads.config2_steady(i) for i in range(a.eval)], log=log)
+        print(json.dumps(dict(train_images=len(samples), epochs=a.epochs, first_loss=hist[0], final_loss=hist[-1],
+                              cases=res)))
+        return
     if a.study_only:
         from . import workloads
 
