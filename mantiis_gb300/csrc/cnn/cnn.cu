@@ -8,6 +8,7 @@
 #include <cstdint>
 
 #include "../../../include/mantiis_cnn.h"
+#include "conv_tc.cuh"
 
 namespace
 {
@@ -252,6 +253,22 @@ int done()
 
 unsigned blocks(int64_t count) { return (unsigned)((count + 255) / 256); }
 
+// the tensor-core convolutions take more than 48 KB of dynamic shared memory
+int tc_attributes()
+{
+    static int rc = 1;
+    if (rc == 1)
+    {
+        cudaError_t e = cudaFuncSetAttribute(cnn_tc::k_conv3x3_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)cnn_tc::kSmemBytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(cnn_tc::k_conv3x3_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cnn_tc::kSmemBytes);
+        rc = e == cudaSuccess ? 0 : -(int)e;
+    }
+    return rc;
+}
+
 dim3 conv_grid(int h, int wd, int groups, int n)
 {
     return dim3((unsigned)(((wd + TS - 1) / TS) * ((h + TS - 1) / TS)), (unsigned)groups, (unsigned)n);
@@ -277,6 +294,41 @@ int cnn_conv3x3_backward_data(const float *dy, const uint16_t *w, float *dx, int
     k_conv3x3<true><<<conv_grid(h, wd, (cin + COB - 1) / COB, n), 256, 0, (cudaStream_t)stream>>>(dy, w, nullptr, dx,
                                                                                                   cout, cin, h, wd, 0);
     return done();
+}
+
+int cnn_conv3x3_forward_tc(const float *x, const uint16_t *w, const float *b, float *y, int n, int cin, int cout,
+                           int h, int wd, int relu, void *stream)
+{
+    if (n <= 0 || cin <= 0 || cout <= 0 || h <= 0 || wd <= 0) return -1;
+    const int rc = tc_attributes();
+    if (rc) return rc;
+    const dim3 grid((unsigned)((h * wd + cnn_tc::kM - 1) / cnn_tc::kM),
+                    (unsigned)((cout + cnn_tc::kNMax - 1) / cnn_tc::kNMax), (unsigned)n);
+    cnn_tc::k_conv3x3_tc<false><<<grid, cnn_tc::kM, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(x, w, b, y, cin, cout,
+                                                                                             h, wd, relu);
+    return done();
+}
+
+int cnn_conv3x3_backward_data_tc(const float *dy, const uint16_t *w, float *dx, int n, int cin, int cout, int h, int wd,
+                                 void *stream)
+{
+    if (n <= 0 || cin <= 0 || cout <= 0 || h <= 0 || wd <= 0) return -1;
+    const int rc = tc_attributes();
+    if (rc) return rc;
+    const dim3 grid((unsigned)((h * wd + cnn_tc::kM - 1) / cnn_tc::kM),
+                    (unsigned)((cin + cnn_tc::kNMax - 1) / cnn_tc::kNMax), (unsigned)n);
+    // a convolution from the cout gradient channels to the cin input channels
+    cnn_tc::k_conv3x3_tc<true><<<grid, cnn_tc::kM, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(dy, w, nullptr, dx, cout,
+                                                                                            cin, h, wd, 0);
+    return done();
+}
+
+int cnn_tc_error(void)
+{
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, cnn_tc::g_tc_error, sizeof(v)) != cudaSuccess) return -1;
+    if (v && cudaMemcpyToSymbol(cnn_tc::g_tc_error, &zero, sizeof(zero)) != cudaSuccess) return -1;
+    return (int)v;
 }
 
 int cnn_conv3x3_backward_weight(const float *x, const float *dy, float *dw, float *db, int n, int cin, int cout, int h,

@@ -33,6 +33,9 @@ _P = C.c_void_p
 _SIG = {
     "cnn_conv3x3_forward": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_conv3x3_backward_data": [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_conv3x3_forward_tc": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_conv3x3_backward_data_tc": [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_tc_error": [],
     "cnn_conv3x3_backward_weight": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_relu_backward": [_P, _P, C.c_int64, _P],
     "cnn_avgpool2_forward": [_P, _P, C.c_int, C.c_int, C.c_int, _P],
