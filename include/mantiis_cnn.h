@@ -27,7 +27,7 @@ int cnn_conv3x3_forward(const float *x, const uint16_t *w, const float *b, float
 /* dx = the gradient of conv3x3 with respect to its input, from dy (cout channels) */
 int cnn_conv3x3_backward_data(const float *dy, const uint16_t *w, float *dx, int n, int cin, int cout, int h, int wd,
                               void *stream);
-/* The same two convolutions as implicit GEMMs on the tensor cores (tcgen05): the FP32
+/* The same convolutions as implicit GEMMs on the tensor cores (tcgen05): the FP32
  * activations are split into two BF16 parts, each multiplied by the BF16 weights with FP32
  * accumulation in tensor memory, so the results agree with the two calls above to FP32
  * rounding.  cnn_tc_error() returns (and clears) the error word those kernels set when a
@@ -36,6 +36,10 @@ int cnn_conv3x3_forward_tc(const float *x, const uint16_t *w, const float *b, fl
                            int h, int wd, int relu, void *stream);
 int cnn_conv3x3_backward_data_tc(const float *dy, const uint16_t *w, float *dx, int n, int cin, int cout, int h, int wd,
                                  void *stream);
+/* the weight gradient the same way (both operands split, three MMAs per step, the
+ * pixels split over CTAs whose partial sums are added to dw atomically) */
+int cnn_conv3x3_backward_weight_tc(const float *x, const float *dy, float *dw, float *db, int n, int cin, int cout,
+                                   int h, int wd, void *stream);
 int cnn_tc_error(void);
 /* dw += sum over batch and pixels of dy * shifted x; db += sum of dy (db may be NULL) */
 int cnn_conv3x3_backward_weight(const float *x, const float *dy, float *dw, float *db, int n, int cin, int cout, int h,

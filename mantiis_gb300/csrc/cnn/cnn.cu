@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "../../../include/mantiis_cnn.h"
@@ -264,9 +265,30 @@ int tc_attributes()
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(cnn_tc::k_conv3x3_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)cnn_tc::kSmemBytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(cnn_tc::k_conv3x3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cnn_tc::kWSmemBytes);
         rc = e == cudaSuccess ? 0 : -(int)e;
     }
     return rc;
+}
+
+// output channels per CTA of the tensor-core convolutions: all (up to 256) when
+// the pixel tiles alone fill the GPU, else fewer (multiples of 16), so that the
+// launch has about two CTAs per SM
+int tc_ntile(int pixel_ctas, int cout)
+{
+    static int sms = 0;
+    if (!sms)
+    {
+        int dev = 0;
+        sms = 148;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    int nt = std::min(cout, cnn_tc::kNMax);
+    nt = (nt + 15) & ~15;
+    while (nt > 16 && (int64_t)pixel_ctas * ((cout + nt - 1) / nt) < 2 * sms) nt = ((nt / 2) + 15) & ~15;
+    return nt;
 }
 
 dim3 conv_grid(int h, int wd, int groups, int n)
@@ -302,10 +324,11 @@ int cnn_conv3x3_forward_tc(const float *x, const uint16_t *w, const float *b, fl
     if (n <= 0 || cin <= 0 || cout <= 0 || h <= 0 || wd <= 0) return -1;
     const int rc = tc_attributes();
     if (rc) return rc;
-    const dim3 grid((unsigned)((h * wd + cnn_tc::kM - 1) / cnn_tc::kM),
-                    (unsigned)((cout + cnn_tc::kNMax - 1) / cnn_tc::kNMax), (unsigned)n);
-    cnn_tc::k_conv3x3_tc<false><<<grid, cnn_tc::kM, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(x, w, b, y, cin, cout,
-                                                                                             h, wd, relu);
+    const int tiles = (h * wd + cnn_tc::kM - 1) / cnn_tc::kM;
+    const int nt = tc_ntile(tiles * n, cout);
+    const dim3 grid((unsigned)tiles, (unsigned)((cout + nt - 1) / nt), (unsigned)n);
+    cnn_tc::k_conv3x3_tc<false><<<grid, cnn_tc::kThreads, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(
+        x, w, b, y, cin, cout, h, wd, relu, nt);
     return done();
 }
 
@@ -315,11 +338,36 @@ int cnn_conv3x3_backward_data_tc(const float *dy, const uint16_t *w, float *dx, 
     if (n <= 0 || cin <= 0 || cout <= 0 || h <= 0 || wd <= 0) return -1;
     const int rc = tc_attributes();
     if (rc) return rc;
-    const dim3 grid((unsigned)((h * wd + cnn_tc::kM - 1) / cnn_tc::kM),
-                    (unsigned)((cin + cnn_tc::kNMax - 1) / cnn_tc::kNMax), (unsigned)n);
+    const int tiles = (h * wd + cnn_tc::kM - 1) / cnn_tc::kM;
+    const int nt = tc_ntile(tiles * n, cin);
+    const dim3 grid((unsigned)tiles, (unsigned)((cin + nt - 1) / nt), (unsigned)n);
     // a convolution from the cout gradient channels to the cin input channels
-    cnn_tc::k_conv3x3_tc<true><<<grid, cnn_tc::kM, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(dy, w, nullptr, dx, cout,
-                                                                                            cin, h, wd, 0);
+    cnn_tc::k_conv3x3_tc<true><<<grid, cnn_tc::kThreads, cnn_tc::kSmemBytes, (cudaStream_t)stream>>>(
+        dy, w, nullptr, dx, cout, cin, h, wd, 0, nt);
+    return done();
+}
+
+int cnn_conv3x3_backward_weight_tc(const float *x, const float *dy, float *dw, float *db, int n, int cin, int cout,
+                                   int h, int wd, void *stream)
+{
+    if (n <= 0 || cin <= 0 || cout <= 0 || h <= 0 || wd <= 0) return -1;
+    const int rc = tc_attributes();
+    if (rc) return rc;
+    const int64_t total = (int64_t)n * h * wd;
+    const int mt = (cout + cnn_tc::kM - 1) / cnn_tc::kM, nt = (cin + cnn_tc::kCC - 1) / cnn_tc::kCC;
+    // split K: about four CTAs per SM over the whole launch, slices of at least
+    // 1024 pixels (a multiple of the 64-pixel chunk)
+    int sms = 148;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t slices = std::max<int64_t>(1, (int64_t)4 * sms / (mt * nt));
+    int64_t slice = (total + slices - 1) / slices;
+    slice = std::max<int64_t>(1024, (slice + cnn_tc::kWK - 1) / cnn_tc::kWK * cnn_tc::kWK);
+    slices = (total + slice - 1) / slice;
+    const dim3 grid((unsigned)mt, (unsigned)nt, (unsigned)slices);
+    cnn_tc::k_conv3x3_wgrad_tc<<<grid, cnn_tc::kThreads, cnn_tc::kWSmemBytes, (cudaStream_t)stream>>>(
+        x, dy, dw, n, cin, cout, h, wd, (int)slice);
+    if (db) cnn_tc::k_bias_grad<<<cout, 256, 0, (cudaStream_t)stream>>>(dy, db, n, cout, h * wd);
     return done();
 }
 

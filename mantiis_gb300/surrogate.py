@@ -28,6 +28,13 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libmantiis_cnn.so"
 _cnn = None
+# True: the convolutions' forward and data gradient run as the tcgen05 implicit
+# GEMMs (cnn_conv3x3_*_tc).  Their operand staging (the threads gather the patch
+# matrix and split it into two BF16 parts in shared memory, one stage) bounds
+# them at 7-12 TFLOP/s, below the CUDA-core kernels' 13-15 at this network's
+# layer sizes (8 x 32..256 channels, 16^2..128^2 pixels), so those stay the
+# default; both agree with FP64 to within 6e-6 of the largest output.
+TENSOR_CORES = False
 
 _P = C.c_void_p
 _SIG = {
@@ -35,6 +42,7 @@ _SIG = {
     "cnn_conv3x3_backward_data": [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_conv3x3_forward_tc": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_conv3x3_backward_data_tc": [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
+    "cnn_conv3x3_backward_weight_tc": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_tc_error": [],
     "cnn_conv3x3_backward_weight": [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P],
     "cnn_relu_backward": [_P, _P, C.c_int64, _P],
@@ -112,8 +120,9 @@ class Conv3x3:
 
         n, _, h, w = x.shape
         y = torch.empty((n, self.cout, h, w), dtype=torch.float32, device="cuda")
-        _check(cnn_lib().cnn_conv3x3_forward(_ptr(x), _ptr(self.w16), _ptr(self.b), _ptr(y), n, self.cin, self.cout,
-                                             h, w, 1 if relu else 0, _stream()), "conv forward")
+        fwd = cnn_lib().cnn_conv3x3_forward_tc if TENSOR_CORES else cnn_lib().cnn_conv3x3_forward
+        _check(fwd(_ptr(x), _ptr(self.w16), _ptr(self.b), _ptr(y), n, self.cin, self.cout, h, w, 1 if relu else 0,
+                   _stream()), "conv forward")
         return y
 
     def backward(self, x, dy, need_dx=True):
@@ -127,8 +136,8 @@ class Conv3x3:
         if not need_dx:
             return None
         dx = torch.empty_like(x)
-        _check(L.cnn_conv3x3_backward_data(_ptr(dy), _ptr(self.w16), _ptr(dx), n, self.cin, self.cout, h, w,
-                                           _stream()), "conv data gradient")
+        bwd = L.cnn_conv3x3_backward_data_tc if TENSOR_CORES else L.cnn_conv3x3_backward_data
+        _check(bwd(_ptr(dy), _ptr(self.w16), _ptr(dx), n, self.cin, self.cout, h, w, _stream()), "conv data gradient")
         return dx
 
     def zero_grad(self):

@@ -75,3 +75,45 @@ def test_tensor_core_conv_matches(shape, transpose):
     record(f"conv_tc_{'bw' if transpose else 'fw'}_{cin}_{cout}_{h}x{wd}", tc=e_tc, cuda_core=e_cc)
     # measured on a GB300: 2.1e-6 .. 5.2e-6 (the CUDA-core kernels 1.3e-7 .. 1.8e-6)
     assert e_tc < 5e-5, (e_tc, e_cc)
+
+
+def wgrad_ref(x, dy):
+    """FP64 weight and bias gradients of a 3x3 convolution (x: input, dy: output gradient)."""
+    n, cin, h, wd = x.shape
+    xp = np.zeros((n, cin, h + 2, wd + 2))
+    xp[:, :, 1:-1, 1:-1] = x
+    dw = np.zeros((dy.shape[1], cin, 3, 3))
+    for ky in range(3):
+        for kx in range(3):
+            dw[:, :, ky, kx] = np.einsum("nohw,nchw->oc", dy, xp[:, :, ky:ky + h, kx:kx + wd])
+    return dw, dy.sum(axis=(0, 2, 3))
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_tensor_core_weight_gradient_matches(shape):
+    import torch
+
+    from mantiis_gb300 import surrogate as S
+
+    n, cin, cout, h, wd = shape
+    rng = np.random.default_rng(cin * 7 + cout)
+    x = rng.standard_normal((n, cin, h, wd)).astype(np.float32)
+    dy = rng.standard_normal((n, cout, h, wd)).astype(np.float32)
+    X, DY = torch.tensor(x, device="cuda"), torch.tensor(dy, device="cuda")
+    L = S.cnn_lib()
+    st = S._stream()
+    out = {}
+    for name, fn in (("tc", L.cnn_conv3x3_backward_weight_tc), ("cc", L.cnn_conv3x3_backward_weight)):
+        dw = torch.zeros(cout * cin * 9, device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        assert fn(S._ptr(X), S._ptr(DY), S._ptr(dw), S._ptr(db), n, cin, cout, h, wd, st) == 0
+        torch.cuda.synchronize()
+        out[name] = (dw.cpu().numpy().reshape(cout, cin, 3, 3), db.cpu().numpy())
+    assert L.cnn_tc_error() == 0
+    ref_w, ref_b = wgrad_ref(x.astype(np.float64), dy.astype(np.float64))
+    e = {k: np.abs(v[0] - ref_w).max() / np.abs(ref_w).max() for k, v in out.items()}
+    e_b = np.abs(out["tc"][1] - ref_b).max() / np.abs(ref_b).max()
+    from test_gpu_transport import record
+
+    record(f"conv_tc_wgrad_{cin}_{cout}_{h}x{wd}", tc=e["tc"], cuda_core=e["cc"], bias=e_b)
+    assert e["tc"] < 5e-5 and e_b < 1e-5, (e, e_b)
