@@ -91,7 +91,8 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
 template <int P>
 __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int diff, int store_u,
                                           int x, int y, int64_t s, const float df[9], float omega, bool special,
-                                          const SpecialRec &rec, double &r_diff, double &r_norm, bool interior = false)
+                                          const SpecialRec &rec, double &r_diff, double &r_norm, bool interior = false,
+                                          const float *unorm_prev = nullptr)
 {
     float drho, rho, ux, uy;
     macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
@@ -100,7 +101,7 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
         const float un = sqrtf(ux * ux + uy * uy);
         if (diff)
         {
-            r_diff = (double)fabsf(un - L.unorm[s]);
+            r_diff = (double)fabsf(un - (unorm_prev ? *unorm_prev : L.unorm[s]));
             r_norm = (double)un;
         }
         if (store_u) L.unorm[s] = un;
@@ -196,10 +197,11 @@ __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, 
         const int64_t s = site_of(L, x, y);
         // (a "direct" state is read like an even step: own slots)
         float df[9];
+        const float uprev = diff ? __ldg(&L.unorm[s]) : 0.0f; // with the populations, as in plain_tile8
         load_raw_ro<P>(L, x, y, df, interior);
         const float om = __ldg(&L.omega[s]);
         SpecialRec none;
-        step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior);
+        step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev);
     }
 }
 
@@ -227,6 +229,9 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
     const int64_t s = site_of(L, x, y);
     float df[9];
     float om;
+    // the |u| the residual compares with, loaded with the populations (the
+    // cell's own site: this thread alone writes it, after reading it)
+    const float uprev = diff ? ldf<NC>(&L.unorm[s]) : 0.0f;
     if (!light)
     {
         load_raw_ro<P, NC>(L, x, y, df, interior);
@@ -261,7 +266,7 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
         }
     }
     SpecialRec none;
-    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev);
 }
 
 // One special cell (wall links, missing arrivals, interface buffer, inlet /
@@ -272,6 +277,9 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
 {
     const SpecialRec rec = C.specials[i];
     const int x = rec.xy & 0xFFFF, y = rec.xy >> 16;
+    const int64_t s = site_of(L, x, y);
+    // the |u| the residual compares with, in flight with the populations
+    const float uprev = diff ? L.unorm[s] : 0.0f;
     float df[9];
     const uint32_t flags = (rec.m1 >> 17) & 0xFu;
     if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
@@ -283,7 +291,7 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
         load_raw<0>(L, x, y, df);
     else
         load_special<P>(L, C, rec, x, y, df);
-    step_cell<P>(L, C, o, diff, store_u, x, y, site_of(L, x, y), df, rec.omega, true, rec, r_diff, r_norm);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, rec.omega, true, rec, r_diff, r_norm, false, &uprev);
 }
 
 // ---- phase kernels.  A coarse time step is a sequence of phases; a phase
@@ -427,6 +435,7 @@ __device__ __forceinline__ void plain_tile_smem(const LevelView &L, const Common
     const int x = (tile & 0xFFFF) * 32 + lx, y = (tile >> 16) * 8 + ly;
     const int64_t s = site_of(L, x, y);
     const float om = som[ly * 32 + lx];
+    const float uprev = diff ? L.unorm[s] : 0.0f;
     float df[9];
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -437,7 +446,7 @@ __device__ __forceinline__ void plain_tile_smem(const LevelView &L, const Common
         df[q] = sb[(pq * kTmaH + sy) * kTmaW + sx];
     }
     SpecialRec none;
-    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, true);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, true, &uprev);
 }
 
 __global__ void __launch_bounds__(256, 4) k_phase_plain_tma(const __grid_constant__ TmaLaunch P)
