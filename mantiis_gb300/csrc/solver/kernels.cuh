@@ -84,6 +84,17 @@ __device__ __forceinline__ float load_cell(const LevelView &L, const Common &C, 
     return -om;
 }
 
+// The coarse-step-start moments (drho, u_x, u_y) of site s.  In a launch that
+// uses them nothing writes them (phase 0 stored them), so the step kernels may
+// take the read-only path (NC); the persistent step, where phase 0 ran earlier
+// in the same launch, takes ordinary loads.
+template <bool NC> __device__ __forceinline__ void load_snap(const LevelView &L, int64_t s, float sn[3])
+{
+    sn[0] = ldf<NC>(&L.snap[s]);
+    sn[1] = ldf<NC>(&L.snap[L.plane + s]);
+    sn[2] = ldf<NC>(&L.snap[2 * L.plane + s]);
+}
+
 // Collision and streaming of one cell whose populations df are loaded:
 // macroscopic moments (and the residual / snapshot side outputs), equilibrium,
 // regularized MRT / MRT / BGK collision, the wall values of special cells and
@@ -92,7 +103,7 @@ template <int P>
 __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, const StepOpt &o, int diff, int store_u,
                                           int x, int y, int64_t s, const float df[9], float omega, bool special,
                                           const SpecialRec &rec, double &r_diff, double &r_norm, bool interior = false,
-                                          const float *unorm_prev = nullptr)
+                                          const float *unorm_prev = nullptr, const float *snap_prev = nullptr)
 {
     float drho, rho, ux, uy;
     macro(df, C.rho0, L.fshift, 0.0f, drho, rho, ux, uy);
@@ -115,10 +126,12 @@ __device__ __forceinline__ void step_cell(const LevelView &L, const Common &C, c
     float edrho = drho, erho = rho, eux = ux, euy = uy;
     if (o.snap_use)
     {
-        edrho = L.snap[s];
+        // the coarse-step-start moments: loaded by the caller with the populations
+        // where it can (a load here is one more dependent round trip per cell)
+        edrho = snap_prev ? snap_prev[0] : L.snap[s];
         erho = C.rho0 + edrho;
-        eux = L.snap[L.plane + s];
-        euy = L.snap[2 * L.plane + s];
+        eux = snap_prev ? snap_prev[1] : L.snap[L.plane + s];
+        euy = snap_prev ? snap_prev[2] : L.snap[2 * L.plane + s];
     }
     float feq[9], fs[9];
     equilibrium(edrho, erho, eux, euy, feq);
@@ -196,12 +209,14 @@ __device__ __forceinline__ void plain_tile(const LevelView &L, const Common &C, 
     {
         const int64_t s = site_of(L, x, y);
         // (a "direct" state is read like an even step: own slots)
-        float df[9];
+        float df[9], sn[3] = {0.f, 0.f, 0.f};
         const float uprev = diff ? __ldg(&L.unorm[s]) : 0.0f; // with the populations, as in plain_tile8
+        if (o.snap_use) load_snap<true>(L, s, sn);
         load_raw_ro<P>(L, x, y, df, interior);
         const float om = __ldg(&L.omega[s]);
         SpecialRec none;
-        step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev);
+        step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev,
+                     o.snap_use ? sn : nullptr);
     }
 }
 
@@ -232,6 +247,8 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
     // the |u| the residual compares with, loaded with the populations (the
     // cell's own site: this thread alone writes it, after reading it)
     const float uprev = diff ? ldf<NC>(&L.unorm[s]) : 0.0f;
+    float sn[3] = {0.f, 0.f, 0.f};
+    if (o.snap_use) load_snap<NC>(L, s, sn);
     if (!light)
     {
         load_raw_ro<P, NC>(L, x, y, df, interior);
@@ -266,7 +283,8 @@ __device__ __forceinline__ void plain_tile8(const LevelView &L, const Common &C,
         }
     }
     SpecialRec none;
-    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, interior, &uprev,
+                 o.snap_use ? sn : nullptr);
 }
 
 // One special cell (wall links, missing arrivals, interface buffer, inlet /
@@ -280,6 +298,8 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
     const int64_t s = site_of(L, x, y);
     // the |u| the residual compares with, in flight with the populations
     const float uprev = diff ? L.unorm[s] : 0.0f;
+    float sn[3] = {0.f, 0.f, 0.f};
+    if (o.snap_use) load_snap<false>(L, s, sn);
     float df[9];
     const uint32_t flags = (rec.m1 >> 17) & 0xFu;
     if ((flags & SF_BUFFER) && (o.first_sub || o.direct))
@@ -291,7 +311,8 @@ __device__ __forceinline__ void special_cell(const LevelView &L, const Common &C
         load_raw<0>(L, x, y, df);
     else
         load_special<P>(L, C, rec, x, y, df);
-    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, rec.omega, true, rec, r_diff, r_norm, false, &uprev);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, rec.omega, true, rec, r_diff, r_norm, false, &uprev,
+                 o.snap_use ? sn : nullptr);
 }
 
 // ---- phase kernels.  A coarse time step is a sequence of phases; a phase
@@ -436,6 +457,8 @@ __device__ __forceinline__ void plain_tile_smem(const LevelView &L, const Common
     const int64_t s = site_of(L, x, y);
     const float om = som[ly * 32 + lx];
     const float uprev = diff ? L.unorm[s] : 0.0f;
+    float sn[3] = {0.f, 0.f, 0.f};
+    if (o.snap_use) load_snap<true>(L, s, sn);
     float df[9];
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -446,7 +469,8 @@ __device__ __forceinline__ void plain_tile_smem(const LevelView &L, const Common
         df[q] = sb[(pq * kTmaH + sy) * kTmaW + sx];
     }
     SpecialRec none;
-    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, true, &uprev);
+    step_cell<P>(L, C, o, diff, store_u, x, y, s, df, om, false, none, r_diff, r_norm, true, &uprev,
+                 o.snap_use ? sn : nullptr);
 }
 
 __global__ void __launch_bounds__(256, 4) k_phase_plain_tma(const __grid_constant__ TmaLaunch P)
