@@ -525,50 +525,61 @@ def main():
     # independent and single-threaded);
     # per image the equilibrium state is uploaded, Ke steps run with the per-step
     # residual and break test, and the cell fields are read back
-    Ke = args.e2e_steps
-    e2e_streams = [torch.cuda.Stream() for _ in solvers]
-    # (the contexts were created with concurrent=1: two of them step at once)
-    for s, st in zip(solvers, e2e_streams):
-        s.set_stream(st.cuda_stream)
+    def e2e_leg(Ke):
+        """Per image (on E2E_THREADS host threads, each context on its own
+        stream): upload of the initial state, Ke steps with the per-step residual
+        and break test, read-back of the cell fields; None when Ke is 0 (for
+        profiled runs, whose multi-threaded host calls the profiler serialises)."""
+        if Ke <= 0:
+            return None
+        e2e_streams = [torch.cuda.Stream() for _ in solvers]
+        # (the contexts were created with concurrent=1: two of them step at once)
+        for s, st in zip(solvers, e2e_streams):
+            s.set_stream(st.cuda_stream)
 
-    # pinned host buffers per image: the initial state and the fields read back
-    pinned = []
-    for s in solvers:
-        n = s.n_cells
-        buf = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
-               for k in ("rho", "ux", "uy", "out_rho", "out_ux", "out_uy")}
-        buf["rho"][:] = s.info["rho_in"]
-        buf["ux"][:] = 0.0
-        buf["uy"][:] = 0.0
-        pinned.append(buf)
+        # pinned host buffers per image: the initial state and the fields read back
+        pinned = []
+        for s in solvers:
+            n = s.n_cells
+            buf = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+                   for k in ("rho", "ux", "uy", "out_rho", "out_ux", "out_uy")}
+            buf["rho"][:] = s.info["rho_in"]
+            buf["ux"][:] = 0.0
+            buf["uy"][:] = 0.0
+            pinned.append(buf)
 
-    def e2e_image(i, steps):
-        s, b = solvers[i], pinned[i]
-        n = s.n_cells
-        s.set_equilibrium(b["rho"], b["ux"], b["uy"])
-        s.run(steps)
-        s.cells(out={"rho": b["out_rho"], "ux": b["out_ux"], "uy": b["out_uy"]})
-        return 3 * n * 8, 3 * n * 8 + steps * 4 * 8
+        def e2e_image(i, steps):
+            s, b = solvers[i], pinned[i]
+            n = s.n_cells
+            s.set_equilibrium(b["rho"], b["ux"], b["uy"])
+            s.run(steps)
+            s.cells(out={"rho": b["out_rho"], "ux": b["out_ux"], "uy": b["out_uy"]})
+            return 3 * n * 8, 3 * n * 8 + steps * 4 * 8
 
-    from concurrent.futures import ThreadPoolExecutor
+        from concurrent.futures import ThreadPoolExecutor
 
-    with ThreadPoolExecutor(min(len(solvers), E2E_THREADS)) as ex:
-        # untimed: plans, checkpoint buffers and the two-step residual graph
-        list(ex.map(lambda i: e2e_image(i, 5), range(len(solvers))))
-        torch.cuda.synchronize()
-        # the whole leg (upload, Ke steps, download of every image) is timed
-        # E2E_REPEATS times from the same initial state; the median is reported,
-        # since one ~60 ms host-timed run is exposed to host-side hiccups
-        e2e_runs = []
-        for _ in range(E2E_REPEATS):
-            t0 = time.perf_counter()
-            moved = list(ex.map(lambda i: e2e_image(i, Ke), range(len(solvers))))
+        with ThreadPoolExecutor(min(len(solvers), E2E_THREADS)) as ex:
+            # untimed: plans, checkpoint buffers and the two-step residual graph
+            list(ex.map(lambda i: e2e_image(i, 5), range(len(solvers))))
             torch.cuda.synchronize()
-            e2e_runs.append(time.perf_counter() - t0)
-        e2e_s = float(np.median(e2e_runs))
-    h2d = sum(m[0] for m in moved)
-    d2h = sum(m[1] for m in moved)
-    e2e = lu_step * Ke / e2e_s / 1e6
+            # the whole leg (upload, Ke steps, download of every image) is timed
+            # E2E_REPEATS times from the same initial state; the median is reported,
+            # since one ~60 ms host-timed run is exposed to host-side hiccups
+            e2e_runs = []
+            for _ in range(E2E_REPEATS):
+                t0 = time.perf_counter()
+                moved = list(ex.map(lambda i: e2e_image(i, Ke), range(len(solvers))))
+                torch.cuda.synchronize()
+                e2e_runs.append(time.perf_counter() - t0)
+            e2e_s = float(np.median(e2e_runs))
+        h2d = sum(m[0] for m in moved)
+        d2h = sum(m[1] for m in moved)
+        e2e = lu_step * Ke / e2e_s / 1e6
+        return {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,
+                "steps": Ke, "seconds": e2e_s, "repeats": len(e2e_runs),
+                "seconds_min_max": [min(e2e_runs), max(e2e_runs)]}
+
+    e2e_obj = e2e_leg(args.e2e_steps)
 
     steady = None
     if rank == 0 and args.steady_images > 0:
@@ -616,9 +627,7 @@ def main():
             "steady_state": steady,
             **({"steady_batch": steady_batch} if steady_batch else {}),
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / Ke, "d2h_bytes_per_step": d2h / Ke,
-                    "steps": Ke, "seconds": e2e_s, "repeats": len(e2e_runs),
-                    "seconds_min_max": [min(e2e_runs), max(e2e_runs)]},
+            "e2e": e2e_obj,
             "clocks": clocks,
             "gpu_launches": int(launches),
         }
