@@ -149,15 +149,23 @@ def params_for(img, plain_path=-1):
                           plain_path=plain_path)
 
 
-def cpu_oracle_rate(img, seconds, threads):
-    """MLUPS of the FP64 oracle on one image, steps sized to ~`seconds`."""
-    from mantiis_gb300 import HostGrid, Solver  # noqa: F401
+def oracle_grid(img):
+    """Grid tables of a benchmark image from the oracle's own restatement of the
+    reference's grid construction (oracle/grid_oracle.cpp): the CPU legs run no
+    product code."""
+    from oracle.pygrid import GridTables
+
+    levels = img.get("levels", 3)
+    return GridTables(img["pore"], img["kn"], img["locpore"], multiblock=levels > 1, max_allowed_level=levels,
+                      edge_fine=levels > 1 and img.get("edge_fine", 1), dx=img["dx"])
+
+
+def cpu_oracle_rate(grid, dx, seconds, threads):
+    """MLUPS of the FP64 oracle on one image's grid, steps sized to ~`seconds`."""
     from oracle.pyoracle import for_grid
 
-    p = params_for(img)
-    g = HostGrid(img["pore"], img["kn"], img["locpore"], p)
-    lu = float(np.sum([(1 << (g.max_level - l)) for l, b in zip(g.cells["level"], g.cells["is_buffer"]) if not b]))
-    o = for_grid(g, sim="transport", dx=img["dx"], threads=threads)
+    lu = grid.lattice_updates()
+    o = for_grid(grid, sim="transport", dx=dx, threads=threads)
     t0 = time.perf_counter()
     o.run(1)
     t1 = time.perf_counter()
@@ -168,6 +176,16 @@ def cpu_oracle_rate(img, seconds, threads):
     dt = time.perf_counter() - t0
     o.close()
     return lu * steps / dt / 1e6, steps, dt, lu
+
+
+def loaded_product_libraries():
+    """Shared objects of this repository's package mapped into this process."""
+    try:
+        maps = Path("/proc/self/maps").read_text()
+    except OSError:
+        return None
+    pkg = str(ROOT / "mantiis_gb300")
+    return sorted({ln.split()[-1] for ln in maps.splitlines() if ln.split()[-1].startswith(pkg)})
 
 
 def job_rate(lu_local, ms_local, steps, dist=None, device="cpu"):
@@ -282,13 +300,15 @@ def run_reference(args, rank, world):
     whole run (warm-up and K samples) stays within about --ref-budget seconds."""
     if rank != 0:
         return
-    from mantiis_gb300 import HostGrid
+    from oracle.pygrid import config2_image
     from oracle.pyoracle import for_grid
 
-    img = make_images(1, 0)[0]
+    # image 0 of the GPU arm's batch (stored as bits in oracle/data); its Kn
+    # field, grid tables and unit system from the oracle's own code
+    img = config2_image(0)
     threads = os.cpu_count() or 1
-    g = HostGrid(img["pore"], img["kn"], img["locpore"], params_for(img))
-    lu = float(np.sum([(1 << (g.max_level - l)) for l, b in zip(g.cells["level"], g.cells["is_buffer"]) if not b]))
+    g = oracle_grid(img)
+    lu = g.lattice_updates()
     o = for_grid(g, sim="transport", dx=img["dx"], threads=threads)
     t0 = time.perf_counter()
     o.run(1)
@@ -310,8 +330,10 @@ def run_reference(args, rank, world):
         "config": {"workload": WORKLOAD, "images": 1, "n": 1024, "levels": 3},
         "cpu_baseline": {"value": rate, "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"image 0, {n} coarse step(s) per step (median of {args.steps}), FP64 oracle "
-                                   f"restatement of the reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads"},
+                                   f"restatement of the reference step (oracle/lbm_oracle.cpp) on the oracle's own "
+                                   f"grid tables (oracle/grid_oracle.cpp), OpenMP {threads} threads"},
         "e2e": {"value": rate, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "product_libraries_loaded": loaded_product_libraries(),
     }
     print(json.dumps(line))
 
@@ -591,12 +613,14 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, steps, dt, lu = cpu_oracle_rate(imgs[0], args.cpu_seconds, threads)
-        rate1, steps1, dt1, _ = cpu_oracle_rate(imgs[0], args.cpu_seconds / 2, 1)
+        og = oracle_grid(imgs[0])
+        rate, steps, dt, lu = cpu_oracle_rate(og, imgs[0]["dx"], args.cpu_seconds, threads)
+        rate1, steps1, dt1, _ = cpu_oracle_rate(og, imgs[0]["dx"], args.cpu_seconds / 2, 1)
         cpu = {"value": rate, "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": f"image 0 of the batch, {steps} coarse steps ({dt:.1f} s), FP64 oracle restatement of the "
-                         f"reference step (oracle/lbm_oracle.cpp), OpenMP {threads} threads; stepping only (the "
-                         f"grid and the initial state are built before the timed steps)",
+                         f"reference step (oracle/lbm_oracle.cpp) on the oracle's own grid tables "
+                         f"(oracle/grid_oracle.cpp), OpenMP {threads} threads; stepping only (the grid and the "
+                         f"initial state are built before the timed steps)",
                "value_1_thread": rate1, "sample_1_thread": f"{steps1} coarse steps ({dt1:.1f} s), 1 thread"}
 
     if rank == 0:

@@ -3,8 +3,9 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
 checker and by bench.py's CPU-baseline leg -- never by the product.
 
-The oracle consumes grid tables (a mantiis_gb300.HostGrid or any object with
-the same attributes) and restates the reference time step in FP64.
+The oracle consumes grid tables (oracle.pygrid.GridTables, a
+mantiis_gb300.HostGrid or any object with the same attributes) and restates
+the reference time step in FP64.
 """
 import ctypes as C
 import subprocess
@@ -49,8 +50,7 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not LIB.exists():
-            build()
+        build()  # make: rebuilds only what is out of date
         L = C.CDLL(str(LIB))
         L.oracle_create.restype = C.c_void_p
         L.oracle_create.argtypes = [C.POINTER(OracleGrid), C.POINTER(OracleParams), C.c_void_p]
@@ -138,8 +138,9 @@ class Oracle:
 
 
 def for_grid(grid, sim="transport", dx=1e-9, T=300.0, P=2.0e6, fbody=1e-8, **kw):
-    """Oracle with the physical constants of (dx, T, P) from the product's unit system."""
-    from mantiis_gb300 import units
+    """Oracle with the physical constants of (dx, T, P) (the oracle's own
+    restatement of the reference's unit system, oracle/pygrid.py)."""
+    from .pygrid import units
 
     u = units(dx, T, P)
     simulation = {"transport": 0, "adsorption": 1, "coupled": 2}[sim]
