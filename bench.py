@@ -357,6 +357,7 @@ def run_adsorption(args):
     torch.cuda.set_stream(stream)
     s = Solver(img["pore"], img["kn"], img["locpore"], p)
     s.set_stream(stream.cuda_stream)
+    s.set_engine(args.ads_engine)
     rng = np.random.default_rng(3000)
     rho = 0.5 + rng.uniform(-1e-3, 1e-3, s.n_cells)
     s.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
@@ -379,9 +380,13 @@ def run_adsorption(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "config3: 512x512 seeded disk image, porosity 0.6, Shan-Chen adsorption, "
                                "exponential psi (rho0 0.5), G -4.5, G_ads -0.5, rho 0.5 +- 1e-3",
-                   "cells": cells, "l2": "state L2-resident (one 512^2 image)"},
+                   "cells": cells, "l2": "state L2-resident (one 512^2 image)",
+                   "engine": "one cooperative launch per call (grid barriers between passes)" if args.ads_engine
+                   else "launches per pass, pairs of steps from a CUDA graph"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "adsorption step (k_ads_psi + k_ads_step)",
+                     "peak_kind": peak_kind,
+                     "kernel": "adsorption step (" + ("k_ads_persistent" if args.ads_engine else
+                                                      "k_ads_psi + k_ads_step") + ")",
                      "bytes_per_unit": 80.0},
         "mass_after": mass,
     }))
@@ -435,6 +440,8 @@ def main():
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--properties", type=int, default=0, metavar="N")
     ap.add_argument("--adsorption", action="store_true", help="time the config-3 adsorption step instead")
+    ap.add_argument("--ads-engine", type=int, default=1, choices=[0, 1],
+                    help="adsorption engine: 1 one cooperative launch per call, 0 launches per pass")
     # plain-cell kernels: -1 times all three at creation (autotune); a fixed
     # path keeps profiled runs, whose timings the profiler distorts, on one path
     ap.add_argument("--plain-path", type=int, default=-1, choices=[-1, 0, 1, 2])

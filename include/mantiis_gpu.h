@@ -246,6 +246,14 @@ int mgpu_batch_set_stream(mgpu_batch *b, void *stream);
 #define MGPU_ENGINE_STREAMS 0
 #define MGPU_ENGINE_PERSISTENT 1
 int mgpu_batch_set_engine(mgpu_batch *b, int engine, int group);
+/* The adsorption step of one context (single level, not coupled): engine 1
+ * (the default) runs the steps of an mgpu_run batch, an mgpu_advance call or an
+ * mgpu_advance_graph call in one cooperative launch, all of its blocks resident,
+ * each of the two passes of a step closed by a grid barrier whose waits are
+ * bounded (about a second, then MGPU_E_DEVICE); engine 0 launches the passes of
+ * every step (pairs of steps replayed from a CUDA graph).  Both give
+ * bit-identical states; transport contexts are not affected. */
+int mgpu_set_engine(mgpu_ctx *ctx, int engine);
 int mgpu_batch_sync(mgpu_batch *b);
 int64_t mgpu_batch_launch_count(const mgpu_batch *b);
 int mgpu_batch_destroy(mgpu_batch *b);

@@ -599,15 +599,27 @@ __device__ __forceinline__ double ads_density(const LevelView &L, const Common &
     return (double)(fabsf(rho - old) / old);
 }
 
-// pass 1 over the plain cells of the active 32x8 tiles (row masks)
-template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
+// pass 1 over the plain cells of active 32x8 tile t (row masks): one block
+template <int P> __device__ __forceinline__ double ads_psi_tile(const LevelView &L, const Common &C, const StepOpt &o, int t)
 {
-    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
-    const uint32_t mask = L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)];
+    const int tile = L.tiles[t]; // tx | ty << 16
+    const uint32_t mask = L.tile_mask[t * 8 + (threadIdx.x >> 5)];
     const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
     const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
-    double rmax = 0.0;
-    if ((mask >> (threadIdx.x & 31)) & 1u) rmax = ads_density<P, false>(L, C, o, x, y);
+    return ((mask >> (threadIdx.x & 31)) & 1u) ? ads_density<P, false>(L, C, o, x, y) : 0.0;
+}
+
+// pass 1 of special record i of the level (i < spec_count)
+template <int P>
+__device__ __forceinline__ double ads_psi_record(const LevelView &L, const Common &C, const StepOpt &o, int64_t rec)
+{
+    const int32_t xy = C.specials[rec].xy;
+    return ads_density<P, true>(L, C, o, xy & 0xFFFF, xy >> 16);
+}
+
+template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
+{
+    const double rmax = ads_psi_tile<P>(L, C, o, (int)blockIdx.x);
     if (o.diff) block_max(rmax, C.red + o.red_slot);
 }
 
@@ -616,12 +628,7 @@ template <int P> __global__ void __launch_bounds__(128) k_ads_psi_special(LevelV
                                                                           int64_t spec_begin, int spec_count)
 {
     const int i = (int)blockIdx.x * 128 + (int)threadIdx.x;
-    double rmax = 0.0;
-    if (i < spec_count)
-    {
-        const int32_t xy = C.specials[spec_begin + i].xy;
-        rmax = ads_density<P, true>(L, C, o, xy & 0xFFFF, xy >> 16);
-    }
+    const double rmax = i < spec_count ? ads_psi_record<P>(L, C, o, spec_begin + i) : 0.0;
     if (o.diff) block_max(rmax, C.red + o.red_slot);
 }
 
@@ -718,13 +725,16 @@ __device__ __forceinline__ void ads_cell(const LevelView &L, const Common &C, co
     store_post<P>(L, x, y, fs);
 }
 
-// Pass 2 over the plain cells of the active 32x8 tiles.  The neighbour
-// pseudopotentials come by warp shuffles: a warp holds one row of a 32x8 tile, each lane loads psi of its column in the rows y-1, y, y+1
+// Pass 2 over the plain cells of active 32x8 tile t: one block.  The
+// neighbour pseudopotentials come by warp shuffles: a warp holds one row of
+// the tile, each lane loads psi of its column in the rows y-1, y, y+1
 // (coalesced), and takes the x-neighbours from the adjacent lanes; the lanes at
 // the ends of the row (and the last image column) load their outer neighbours.
-template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
+template <int P>
+__device__ __forceinline__ void ads_step_tile(const LevelView &L, const Common &C, const StepOpt &o, int t, double &r_diff,
+                                              double &r_norm)
 {
-    const int tile = L.tiles[blockIdx.x]; // tx | ty << 16
+    const int tile = L.tiles[t]; // tx | ty << 16
     const int lane = threadIdx.x & 31;
     const int x = (tile & 0xFFFF) * 32 + lane;
     const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
@@ -740,31 +750,40 @@ template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, 
         if (inside && lane == 0) psi[r][0] = L.psi[site_of(L, wrapx(x - 1, L.W), yr)];
         if (inside && (lane == 31 || x + 1 == L.W)) psi[r][2] = L.psi[site_of(L, wrapx(x + 1, L.W), yr)];
     }
-    double r_diff = 0.0, r_norm = 0.0;
-    const uint32_t mask = L.tile_mask[blockIdx.x * 8 + (threadIdx.x >> 5)];
+    const uint32_t mask = L.tile_mask[t * 8 + (threadIdx.x >> 5)];
     if ((mask >> lane) & 1u) ads_cell<P, false>(L, C, o, x, y, psi, r_diff, r_norm);
+}
+
+// pass 2 of special record rec; the neighbour pseudopotentials are read directly
+template <int P>
+__device__ __forceinline__ void ads_step_record(const LevelView &L, const Common &C, const StepOpt &o, int64_t rec,
+                                                double &r_diff, double &r_norm)
+{
+    const int32_t xy = C.specials[rec].xy;
+    const int x = xy & 0xFFFF, y = xy >> 16;
+    float psi[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            psi[r][c] = L.psi[site_of(L, wrapx(x + c - 1, L.W), wrapx(y + r - 1, L.H))];
+    ads_cell<P, true>(L, C, o, x, y, psi, r_diff, r_norm);
+}
+
+template <int P> __global__ void __launch_bounds__(256) k_ads_step(LevelView L, Common C, StepOpt o)
+{
+    double r_diff = 0.0, r_norm = 0.0;
+    ads_step_tile<P>(L, C, o, (int)blockIdx.x, r_diff, r_norm);
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 
-// pass 2 over the special cells, from their records; the neighbour
-// pseudopotentials are read directly
+// pass 2 over the special cells, from their records (128 per block)
 template <int P> __global__ void __launch_bounds__(128) k_ads_step_special(LevelView L, Common C, StepOpt o,
                                                                            int64_t spec_begin, int spec_count)
 {
     const int i = (int)blockIdx.x * 128 + (int)threadIdx.x;
     double r_diff = 0.0, r_norm = 0.0;
-    if (i < spec_count)
-    {
-        const int32_t xy = C.specials[spec_begin + i].xy;
-        const int x = xy & 0xFFFF, y = xy >> 16;
-        float psi[3][3];
-#pragma unroll
-        for (int r = 0; r < 3; r++)
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-                psi[r][c] = L.psi[site_of(L, wrapx(x + c - 1, L.W), wrapx(y + r - 1, L.H))];
-        ads_cell<P, true>(L, C, o, x, y, psi, r_diff, r_norm);
-    }
+    if (i < spec_count) ads_step_record<P>(L, C, o, spec_begin + i, r_diff, r_norm);
     if (o.diff) block_add2(r_diff, r_norm, C.red + o.red_slot);
 }
 
@@ -1200,6 +1219,97 @@ __global__ void __launch_bounds__(kPersistThreads, MINB) k_step_persistent(const
         // of the counter then sees them
         __syncthreads();
         if (threadIdx.x == 0) add_release(P.sync + 1 + __ldg(&P.segs[seg].done_ctr), 1u);
+    }
+}
+
+// ---- the adsorption step as one cooperative launch over many steps.  Each
+// step is the two passes of k_ads_psi / k_ads_psi_special and k_ads_step /
+// k_ads_step_special over the same units (32x8 tiles, then runs of 256 special
+// records), walked by a grid that is resident as a whole (cooperative launch);
+// a grid barrier closes each pass.  The per-cell arithmetic is the same code,
+// so the states are bit-identical to the launch-per-pass engine.
+struct AdsPersist
+{
+    LevelView L;
+    Common C;
+    int64_t spec_begin;
+    int spec_count, ntiles;
+    int nsteps, parity0, direct0;
+    int slot0, ring;        // residual of step k in slot (slot0 + k) mod ring
+    int psi_diff, step_diff; // the residual terms of pass 1 (density change) / pass 2 (|u|)
+    unsigned int *bar;      // arrivals at the grid barriers; zero at launch
+};
+
+// Grid barrier `target` = (barriers passed) x gridDim.x: every block adds one
+// arrival with release semantics after its block barrier, then waits (bounded)
+// for all of them; a wait that runs out sets the error word and the block stops.
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, unsigned int target, unsigned int *err)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        add_release(bar, 1u);
+        const bool ok = wait_counter(bar, target);
+        if (!ok) atomicOr(err, kErrDepTimeout);
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+constexpr int kAdsRecords = 256; // special records per unit of k_ads_persistent
+
+__global__ void __launch_bounds__(256) k_ads_persistent(const __grid_constant__ AdsPersist A)
+{
+    const int units = A.ntiles + (A.spec_count + kAdsRecords - 1) / kAdsRecords;
+    unsigned int target = 0;
+    for (int k = 0; k < A.nsteps; k++)
+    {
+        StepOpt o{};
+        o.parity = (A.parity0 + k) & 1;
+        o.direct = k == 0 ? A.direct0 : 0;
+        o.red_slot = ((A.slot0 + k) % A.ring) * 4;
+        o.snap_store = 1;
+        StepOpt o1 = o, o2 = o;
+        o1.diff = A.psi_diff;
+        o2.diff = A.step_diff;
+        for (int u = (int)blockIdx.x; u < units; u += (int)gridDim.x)
+        {
+            double rmax = 0.0;
+            if (u < A.ntiles) rmax = o.parity ? ads_psi_tile<1>(A.L, A.C, o1, u) : ads_psi_tile<0>(A.L, A.C, o1, u);
+            else
+            {
+                const int i = (u - A.ntiles) * kAdsRecords + (int)threadIdx.x;
+                if (i < A.spec_count)
+                    rmax = o.parity ? ads_psi_record<1>(A.L, A.C, o1, A.spec_begin + i)
+                                    : ads_psi_record<0>(A.L, A.C, o1, A.spec_begin + i);
+            }
+            if (o1.diff) block_max(rmax, A.C.red + o1.red_slot);
+        }
+        target += gridDim.x;
+        if (!grid_barrier(A.bar, target, A.C.err)) return;
+        for (int u = (int)blockIdx.x; u < units; u += (int)gridDim.x)
+        {
+            double r_diff = 0.0, r_norm = 0.0;
+            if (u < A.ntiles)
+            {
+                if (o.parity) ads_step_tile<1>(A.L, A.C, o2, u, r_diff, r_norm);
+                else ads_step_tile<0>(A.L, A.C, o2, u, r_diff, r_norm);
+            }
+            else
+            {
+                const int i = (u - A.ntiles) * kAdsRecords + (int)threadIdx.x;
+                if (i < A.spec_count)
+                {
+                    if (o.parity) ads_step_record<1>(A.L, A.C, o2, A.spec_begin + i, r_diff, r_norm);
+                    else ads_step_record<0>(A.L, A.C, o2, A.spec_begin + i, r_diff, r_norm);
+                }
+            }
+            if (o2.diff) block_add2(r_diff, r_norm, A.C.red + o2.red_slot);
+        }
+        target += gridDim.x;
+        if (!grid_barrier(A.bar, target, A.C.err)) return;
     }
 }
 

@@ -250,6 +250,12 @@ struct mgpu_ctx
     DevBuf<double> out_rho, out_ux, out_uy, out_f;
     DevBuf<double> in_rho, in_ux, in_uy; // staging of mgpu_set_equilibrium, kept between calls
     DevBuf<unsigned int> errword;
+    // adsorption step engine: MGPU_ENGINE_PERSISTENT runs many steps in one
+    // cooperative launch (k_ads_persistent), MGPU_ENGINE_STREAMS launches the
+    // passes (pairs of steps replayed from a CUDA graph)
+    int engine = MGPU_ENGINE_PERSISTENT;
+    DevBuf<unsigned int> ads_bar; // grid-barrier arrivals of k_ads_persistent
+    int ads_grid = 0;             // its blocks: all resident at once
     float rho0f = 0.f;
     bool adsorption = false; // Shan-Chen step body (include/mantiisApp.hpp:248-265)
     // coupled run (include/mantiisApp.hpp:376-392): up to 100 adsorption steps
@@ -774,6 +780,57 @@ void run_pair_graph(mgpu_ctx *ctx, bool store_u, int first)
         CK(cudaMemcpyAsync(ctx->red.p, scratch + 4, 4 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
 }
 
+// Adsorption steps k .. k + n - 1 of a single-level context (not coupled) in
+// one cooperative launch; with diff, the residual of step j lands in slot
+// j mod kRing (zeroed by the caller).
+bool ads_persistent_ok(const mgpu_ctx *ctx)
+{
+    return ctx->adsorption && !ctx->coupled && ctx->engine == MGPU_ENGINE_PERSISTENT &&
+           !ctx->lay.levels[0].tile_list.empty();
+}
+
+void run_ads_persistent(mgpu_ctx *ctx, int n, int64_t k, bool diff)
+{
+    // the barrier count of one launch stays far below 2^32 (2 per step and block)
+    constexpr int kMaxSteps = 100000;
+    while (n > kMaxSteps)
+    {
+        run_ads_persistent(ctx, kMaxSteps, k, diff);
+        n -= kMaxSteps;
+        k += kMaxSteps;
+    }
+    const LevelLayout &ll = ctx->lay.levels[0];
+    dev::AdsPersist A{};
+    A.L = ctx->view(0);
+    A.C = ctx->common();
+    A.spec_begin = ll.spec_begin;
+    A.spec_count = (int)ll.spec_count;
+    A.ntiles = (int)ll.tile_list.size();
+    A.nsteps = n;
+    A.parity0 = (int)(ctx->lv[0].steps & 1);
+    A.direct0 = ctx->lv[0].steps == 0 ? 1 : 0;
+    A.slot0 = (int)(k % kRing);
+    A.ring = kRing;
+    A.psi_diff = diff ? 1 : 0; // the density change (the coupling phase, with |u| sums, is not run here)
+    A.step_diff = 0;
+    A.bar = ctx->ads_bar.p;
+    const int units = A.ntiles + (A.spec_count + dev::kAdsRecords - 1) / dev::kAdsRecords;
+    if (ctx->ads_grid == 0)
+    {
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::k_ads_persistent, 256, 0));
+        ctx->ads_grid = std::max(1, per_sm) * ctx->sm_count;
+    }
+    const int grid = std::min(units, ctx->ads_grid);
+    CK(cudaMemsetAsync(A.bar, 0, sizeof(unsigned int), ctx->stream));
+    void *args[] = {&A};
+    CK(cudaLaunchCooperativeKernel((const void *)dev::k_ads_persistent, dim3((unsigned)grid), dim3(256), args, 0,
+                                   ctx->stream));
+    ctx->launches++;
+    ctx->lv[0].steps += n;
+    ctx->coarse_done += n;
+}
+
 bool fresh_state(const mgpu_ctx *ctx)
 {
     for (auto &l : ctx->lv)
@@ -794,6 +851,11 @@ void run_batch_with_residuals(mgpu_ctx *ctx, int n)
     if (ctx->adsorption)
     {
         // the density change of step k is known within step k
+        if (ads_persistent_ok(ctx) && n > 0)
+        {
+            run_ads_persistent(ctx, n, ctx->coarse_done + 1, true);
+            return;
+        }
         for (int i = 0; i < n;)
         {
             int64_t k = ctx->coarse_done + 1;
@@ -1524,6 +1586,7 @@ static int create_impl(const PoreImage &img, const mgpu_params *p, mgpu_ctx **ou
     ctx->red.zero(s);
     ctx->errword.alloc(1, acct);
     ctx->errword.zero(s);
+    if (ctx->adsorption) ctx->ads_bar.alloc(1, acct);
     for (auto &it : ctx->lay.interfaces)
     {
         ctx->itf.emplace_back();
@@ -1720,7 +1783,16 @@ int mgpu_advance(mgpu_ctx *ctx, int n_steps)
             }
             if (ctx->adsorption)
             {
-                if (pairs_ok(i))
+                if (K == 1 && ads_persistent_ok(ctx))
+                {
+                    // the rest of the call (as many steps as the pending slots hold) in one launch
+                    const int m = std::min(n_steps - i, kRing / 2 - (int)pending.size());
+                    zero_slots(ctx, (int)(k % kRing), m);
+                    run_ads_persistent(ctx, m, k, true);
+                    for (int j = 0; j < m; j++) pending.push_back(k + j);
+                    i += m - 1;
+                }
+                else if (pairs_ok(i))
                 {
                     run_pair_graph(ctx, false, (int)(k % kRing));
                     pending.push_back(k);
@@ -1767,6 +1839,12 @@ int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
     if (ctx && ctx->coupled) return mgpu_advance(ctx, n_steps); // its phase switch is host-side
     return guarded(ctx, [&]() {
         if (!ctx || n_steps < 0) throw std::invalid_argument("bad argument");
+        if (ads_persistent_ok(ctx))
+        {
+            if (n_steps > 0) run_ads_persistent(ctx, n_steps, ctx->coarse_done + 1, false);
+            ctx->ref_t += n_steps;
+            return MGPU_OK;
+        }
         int left = n_steps;
         // the graph starts from a stepped state (not the initial "direct" one)
         bool fresh = false;
@@ -1830,6 +1908,16 @@ int mgpu_advance_graph(mgpu_ctx *ctx, int n_steps)
         }
         if (left == 1) coarse_step(ctx, false, false, 0);
         ctx->ref_t += n_steps;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_set_engine(mgpu_ctx *ctx, int engine)
+{
+    return guarded(ctx, [&]() {
+        if (!ctx || (engine != MGPU_ENGINE_STREAMS && engine != MGPU_ENGINE_PERSISTENT))
+            throw std::invalid_argument("bad argument");
+        ctx->engine = engine;
         return MGPU_OK;
     });
 }

@@ -105,6 +105,7 @@ SIGNATURES = {
     "mgpu_batch_observables": (C.c_int, [P, F64P]),
     "mgpu_batch_set_stream": (C.c_int, [P, P]),
     "mgpu_batch_set_engine": (C.c_int, [P, C.c_int, C.c_int]),
+    "mgpu_set_engine": (C.c_int, [P, C.c_int]),
     "mgpu_batch_sync": (C.c_int, [P]),
     "mgpu_batch_launch_count": (C.c_int64, [P]),
     "mgpu_batch_destroy": (C.c_int, [P]),
@@ -313,6 +314,11 @@ class Solver:
     def advance_graph(self, n_steps):
         """Enqueues n coarse steps from a captured CUDA graph; returns without waiting."""
         self._check(lib().mgpu_advance_graph(self._h, int(n_steps)))
+
+    def set_engine(self, engine):
+        """Adsorption step engine (mgpu_set_engine): 1 (default) the steps of a
+        call in one cooperative launch, 0 launches per pass."""
+        self._check(lib().mgpu_set_engine(self._h, int(engine)))
 
     def step_level(self, level, n):
         """Profiling aid: n substeps of one level alone (see mgpu_step_level)."""

@@ -142,3 +142,43 @@ def test_adsorption_disk_image_vs_reference_code():
     e_rho = np.abs(c["rho"] - st["rho"]).max() / np.abs(st["rho"]).max()
     record("adsorption_disk128_vs_reference_100", ux=e_ux, rho=e_rho)
     assert e_ux < 1e-5 and e_rho < 1.5e-5  # measured u_x 9.0e-7, rho 1.4e-6
+
+
+@pytest.mark.parametrize("call", ["run", "advance", "advance_graph"])
+def test_persistent_adsorption_engine_bit_identical(call):
+    # the cooperative launch over many steps (engine 1, the default) and the
+    # launches per pass (engine 0) step the same arithmetic: bit-identical
+    # states and, for run / advance, the same per-step residuals; on a 512^2
+    # config-3 image from a perturbed state, odd step counts (both parities)
+    from mantiis_gb300 import workloads
+
+    img = workloads.config3(0)
+    kw = dict(psi_form=1, rho_psi=0.5, g_ff=-4.5 / 18, g_fs=-1.5)
+    p = default_params(dx=img["dx"], simulation=SIM_ADSORPTION, rho_init=0.5, fbody=0.0, tol=0.0, **kw)
+    rng = np.random.default_rng(3001)
+    out = {}
+    for engine in (0, 1):
+        s = Solver(img["pore"], img["kn"], img["locpore"], p)
+        s.set_engine(engine)
+        n = s.info["n_cells"]
+        rho = 0.5 + rng.uniform(-1e-3, 1e-3, n) if engine == 0 else out[0][2]
+        s.set_equilibrium(rho, np.zeros(n), np.zeros(n))
+        if call == "run":
+            assert s.run(37) == 37
+            assert s.run(1000) == 1000
+        elif call == "advance":
+            s.advance(37)
+            s.advance(1000)
+        else:
+            s.advance_graph(37)
+            s.advance_graph(1000)
+        s.sync()
+        launches = s.launches
+        out[engine] = (s.cells(with_f=True)["f"], s.residuals(), rho, launches)
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    if call != "advance_graph":
+        assert len(out[0][1]) == len(out[1][1]) == 1037
+        assert np.array_equal(out[0][1], out[1][1])
+    # one launch per call (and its barrier reset) against four per step
+    assert out[1][3] < out[0][3] / 100
