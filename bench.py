@@ -130,6 +130,33 @@ WORKLOADS = {
 }
 
 
+def lpt_partition(costs, world):
+    """Greedy longest-processing-time split of independent images over ranks:
+    the costliest image first, each to the rank with the least work so far
+    (the lowest rank on ties).  Returns each rank's image indices, ascending."""
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda k: (-costs[k], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def rank_images(count, rank, world, workload="config2"):
+    """This rank's images.  Equal-cost workloads: rank r takes images
+    r*count .. r*count+count-1; config 4 (sides 128-2048): the count*world
+    images are split by the greedy LPT rule on their pixel counts, so that the
+    slowest rank, which sets the job's time, has as little as possible."""
+    if workload != "config4" or world == 1:
+        return make_images(count, rank * count, workload)
+    from mantiis_gb300 import workloads
+
+    costs = [float(workloads.config4_side(i)) ** 2 for i in range(count * world)]
+    mine = lpt_partition(costs, world)[rank]
+    return [workloads.config4(i) for i in mine]
+
+
 def make_images(count, offset, workload="config2"):
     from mantiis_gb300 import workloads
 
@@ -471,7 +498,7 @@ def main():
         dist.init_process_group("nccl")
     from mantiis_gb300 import Batch, Solver
 
-    imgs = make_images(args.images, rank * args.images, args.workload)
+    imgs = rank_images(args.images, rank, world, args.workload)
     # a dedicated (non-default) stream: every context enqueues on it and the
     # CUDA events below are recorded on it
     stream = torch.cuda.Stream()

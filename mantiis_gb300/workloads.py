@@ -90,6 +90,12 @@ def config3(index=0):
     return image(512, 6, 40, 0.6, 0.1, 3000 + index)
 
 
+def config4_side(index=0):
+    """The side of config-4 image `index` (the generator's first draw), without
+    generating the image: the cost estimate of the multi-GPU partition."""
+    return int(np.random.default_rng(4000 + index).choice([128, 256, 512, 1024, 2048]))
+
+
 def config4(index=0):
     rng = np.random.default_rng(4000 + index)
     n = int(rng.choice([128, 256, 512, 1024, 2048]))

@@ -60,3 +60,27 @@ def test_ranks_own_distinct_images():
     a = bench.make_images(1, 0 * 1, "config2")[0]
     b = bench.make_images(1, 1 * 1, "config2")[0]
     assert (a["pore"] != b["pore"]).any()
+
+
+def test_lpt_partition_balances_uneven_images():
+    import bench
+    from mantiis_gb300 import workloads
+
+    # Graham's tight example for 3 ranks: jobs 5 5 4 4 3 3 3 -> LPT loads 8 / 8 / 11
+    # (the optimum is 9 / 9 / 9; LPT stays within 4/3 - 1/(3m) of it)
+    jobs = [5, 5, 4, 4, 3, 3, 3]
+    parts = bench.lpt_partition(jobs, 3)
+    assert parts == [[0, 4, 6], [1, 5], [2, 3]]
+    assert sorted(sum(jobs[i] for i in p) for p in parts) == [8, 8, 11]
+    # config 4 over 4 ranks: every image exactly once, and the largest rank load
+    # no worse than a contiguous split's
+    count, world = 8, 4
+    costs = [float(workloads.config4_side(i)) ** 2 for i in range(count * world)]
+    parts = bench.lpt_partition(costs, world)
+    assert sorted(i for p in parts for i in p) == list(range(count * world))
+    lpt_max = max(sum(costs[i] for i in p) for p in parts)
+    contiguous_max = max(sum(costs[r * count:(r + 1) * count]) for r in range(world))
+    assert lpt_max <= contiguous_max
+    assert lpt_max <= sum(costs) / world + max(costs)
+    # the side draw is the generator's own first draw
+    assert workloads.config4_side(3) == workloads.config4(3)["pore"].shape[0]
