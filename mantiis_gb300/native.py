@@ -448,6 +448,8 @@ class Batch:
     def __init__(self, solvers):
         self._h = None
         self.solvers = list(solvers)
+        self.stream = None  # as last set (set_stream)
+        self.engine = None  # (engine, group) as last set (set_engine)
         arr = (P * len(self.solvers))(*[s._h for s in self.solvers])
         h = C.c_void_p()
         rc = lib().mgpu_batch_create(arr, len(self.solvers), C.byref(h))
@@ -471,12 +473,14 @@ class Batch:
 
     def set_stream(self, stream_handle):
         self._check(lib().mgpu_batch_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
+        self.stream = stream_handle
 
     def set_engine(self, engine, group=0):
         """engine 0: per-image phase launches on concurrent streams; 1: one
         persistent launch per coarse step over all images (mgpu_batch_set_engine),
         interleaving `group` images at a time (0 = all)."""
         self._check(lib().mgpu_batch_set_engine(self._h, int(engine), int(group)))
+        self.engine = (int(engine), int(group))
 
     def sync(self):
         self._check(lib().mgpu_batch_sync(self._h))

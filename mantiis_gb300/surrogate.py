@@ -327,25 +327,57 @@ def run_to_steady(solver, chunk=1000, tol=1e-6, max_steps=200000):
     return steps, secs, k_old
 
 
-def run_batch_to_steady(batch, chunk=1000, tol=1e-6, max_steps=200000):
-    """run_to_steady for a batch: all images advance together until each one's
-    permeability has settled (settled images keep stepping).  Returns per image
-    the step count at which it settled (max_steps if never) and the permeabilities."""
+def run_batch_to_steady(batch, chunk=1000, tol=1e-6, max_steps=200000, drop_settled=True, stats=None):
+    """run_to_steady for a batch: the images advance together, `chunk` steps at a
+    time, until each one's permeability has settled (relative change <= tol over
+    a chunk).  With drop_settled an image leaves the batch when it settles (the
+    rest continue in a batch of their own, on the same stream and engine), so its
+    state is the one at which it settled and it costs no further GPU time; else
+    settled images keep stepping with the rest.  Returns per image the step
+    count at which it settled (max_steps if never) and the permeabilities; `stats`
+    (a dict) receives the lattice updates done ("lu") and the batches built."""
+    from .native import Batch
+
+    solvers = list(batch.solvers)
+    n = len(solvers)
+    lu_of = np.array([float(s.info["lu_per_step"]) for s in solvers])
     k_old = np.array([o["permeability"] for o in batch.observables()])
-    n = len(k_old)
+    k_now = k_old.copy()
     done = np.zeros(n, bool)
     steps_at = np.full(n, max_steps)
+    active = np.arange(n)
+    cur, own = batch, False
+    lu, batches = 0.0, 1
     steps = 0
-    while steps < max_steps and not done.all():
-        batch.advance(chunk)
-        batch.sync()
-        steps += chunk
-        k = np.array([o["permeability"] for o in batch.observables()])
-        newly = (~done) & np.isfinite(k) & (k != 0) & (np.abs(k - k_old) <= tol * np.abs(k))
-        steps_at[newly] = steps
-        done |= newly
-        k_old = k
-    return steps_at, k_old
+    try:
+        while steps < max_steps and not done.all():
+            cur.advance(chunk)
+            cur.sync()
+            steps += chunk
+            lu += chunk * lu_of[active].sum()
+            k = np.array([o["permeability"] for o in cur.observables()])
+            newly = (~done[active]) & np.isfinite(k) & (k != 0) & (np.abs(k - k_old[active]) <= tol * np.abs(k))
+            steps_at[active[newly]] = steps
+            done[active[newly]] = True
+            k_now[active] = k
+            k_old[active] = k
+            if drop_settled and newly.any() and not done.all():
+                active = active[~newly]
+                nxt = Batch([solvers[i] for i in active])
+                if batch.stream is not None:
+                    nxt.set_stream(batch.stream)
+                if batch.engine is not None:
+                    nxt.set_engine(*batch.engine)
+                if own:
+                    cur.close()
+                cur, own = nxt, True
+                batches += 1
+    finally:
+        if own:
+            cur.close()
+    if stats is not None:
+        stats.update(lu=lu, batches=batches)
+    return steps_at, k_now
 
 
 def target_scale(targets, masks):

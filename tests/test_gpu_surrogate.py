@@ -125,3 +125,37 @@ def test_warm_start_needs_the_density():
     assert sc < 200000
     assert exact <= 0.2 * sc
     assert velocity_only >= 0.9 * sc
+
+
+def test_settled_images_leave_the_batch():
+    # six small config-4 steady images (sides 128 / 256) run to steady state
+    # twice: once with every image stepped to the end, once with each image
+    # leaving the batch when it settles.  An image's arithmetic does not depend
+    # on the batch around it, so both runs see every image settle at the same
+    # step, with the same permeability then; dropping them saves lattice updates
+    from mantiis_gb300 import Batch, Solver, workloads
+    from mantiis_gb300.surrogate import run_batch_to_steady, solver_params
+
+    imgs = [workloads.config4_steady(i) for i in (5, 6, 9, 10, 11, 12)]
+    out = {}
+    for drop in (False, True):
+        sol = [Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, concurrent=1)) for d in imgs]
+        b = Batch(sol)
+        stats = {}
+        steps, k = run_batch_to_steady(b, chunk=1000, tol=1e-6, max_steps=60000, drop_settled=drop, stats=stats)
+        k_settled = np.array([s.observables()["permeability"] for s in sol])
+        out[drop] = (steps, k, k_settled, stats)
+        b.close()
+        for s in sol:
+            s.close()
+    (st0, k0, _, s0), (st1, k1, ks1, s1) = out[False], out[True]
+    assert np.array_equal(st0, st1)
+    assert (st1 < 60000).sum() >= 4
+    settled = st1 < 60000
+    # dropped images hold their state at the settling step: the returned k is
+    # theirs (FP64 atomic sums: equal to 1e-12)
+    assert np.allclose(k1[settled], ks1[settled], rtol=1e-12, atol=0)
+    # stepped on, a settled image's permeability moves by less than the criterion per chunk
+    extra = (st0.max() - st1[settled]) / 1000.0
+    assert np.all(np.abs(k0[settled] - k1[settled]) <= 1e-6 * np.abs(k1[settled]) * (extra + 1))
+    assert s1["lu"] < s0["lu"] and s1["batches"] > 1
