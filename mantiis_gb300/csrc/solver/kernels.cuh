@@ -548,22 +548,24 @@ __global__ void __launch_bounds__(256, 4) k_phase_plain_tma(const __grid_constan
     }
 }
 
-// Maximum of a non-negative double over the block, then one atomic per block
+// Maximum of a non-negative float over the block, then one atomic per block on
+// the double it converts to: the conversion is exact and monotone, so this is
+// the maximum of the converted values, with the shuffles on the FP32 pipe
 // (non-negative doubles order like their bit patterns).
-__device__ __forceinline__ void block_max(double v, double *dst)
+__device__ __forceinline__ void block_max(float v, double *dst)
 {
-    __shared__ double sm[32];
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    __shared__ float sm[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) sm[wid] = v;
     __syncthreads();
     if (wid == 0)
     {
         const int nw = blockDim.x >> 5;
-        v = lane < nw ? sm[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-        if (lane == 0 && v > 0.0)
-            atomicMax(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__double_as_longlong(v));
+        v = lane < nw ? sm[lane] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0f)
+            atomicMax(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__double_as_longlong((double)v));
     }
     __syncthreads();
 }
@@ -575,7 +577,7 @@ __device__ __forceinline__ void block_max(double v, double *dst)
 // density and pseudopotential of one cell (pass 1), the density change against
 // the previous step's density for the residual
 template <int P, bool SPEC>
-__device__ __forceinline__ double ads_density(const LevelView &L, const Common &C, const StepOpt &o, int x, int y)
+__device__ __forceinline__ float ads_density(const LevelView &L, const Common &C, const StepOpt &o, int x, int y)
 {
     const int64_t s = site_of(L, x, y);
     float df[9];
@@ -596,22 +598,22 @@ __device__ __forceinline__ double ads_density(const LevelView &L, const Common &
     L.psi[s] = pseudo_potential((float)C.psi_form, C.psi_rho0, C.eos_a, C.eos_b, C.eos_T, C.g_ff, rho);
     const float old = L.rho_prev[s];
     L.rho_prev[s] = rho;
-    return (double)(fabsf(rho - old) / old);
+    return fabsf(rho - old) / old;
 }
 
 // pass 1 over the plain cells of active 32x8 tile t (row masks): one block
-template <int P> __device__ __forceinline__ double ads_psi_tile(const LevelView &L, const Common &C, const StepOpt &o, int t)
+template <int P> __device__ __forceinline__ float ads_psi_tile(const LevelView &L, const Common &C, const StepOpt &o, int t)
 {
     const int tile = L.tiles[t]; // tx | ty << 16
     const uint32_t mask = L.tile_mask[t * 8 + (threadIdx.x >> 5)];
     const int x = (tile & 0xFFFF) * 32 + (threadIdx.x & 31);
     const int y = (tile >> 16) * 8 + (threadIdx.x >> 5);
-    return ((mask >> (threadIdx.x & 31)) & 1u) ? ads_density<P, false>(L, C, o, x, y) : 0.0;
+    return ((mask >> (threadIdx.x & 31)) & 1u) ? ads_density<P, false>(L, C, o, x, y) : 0.0f;
 }
 
 // pass 1 of special record i of the level (i < spec_count)
 template <int P>
-__device__ __forceinline__ double ads_psi_record(const LevelView &L, const Common &C, const StepOpt &o, int64_t rec)
+__device__ __forceinline__ float ads_psi_record(const LevelView &L, const Common &C, const StepOpt &o, int64_t rec)
 {
     const int32_t xy = C.specials[rec].xy;
     return ads_density<P, true>(L, C, o, xy & 0xFFFF, xy >> 16);
@@ -619,7 +621,7 @@ __device__ __forceinline__ double ads_psi_record(const LevelView &L, const Commo
 
 template <int P> __global__ void __launch_bounds__(256) k_ads_psi(LevelView L, Common C, StepOpt o)
 {
-    const double rmax = ads_psi_tile<P>(L, C, o, (int)blockIdx.x);
+    const float rmax = ads_psi_tile<P>(L, C, o, (int)blockIdx.x);
     if (o.diff) block_max(rmax, C.red + o.red_slot);
 }
 
@@ -628,7 +630,7 @@ template <int P> __global__ void __launch_bounds__(128) k_ads_psi_special(LevelV
                                                                           int64_t spec_begin, int spec_count)
 {
     const int i = (int)blockIdx.x * 128 + (int)threadIdx.x;
-    const double rmax = i < spec_count ? ads_psi_record<P>(L, C, o, spec_begin + i) : 0.0;
+    const float rmax = i < spec_count ? ads_psi_record<P>(L, C, o, spec_begin + i) : 0.0f;
     if (o.diff) block_max(rmax, C.red + o.red_slot);
 }
 
@@ -1276,7 +1278,7 @@ __global__ void __launch_bounds__(256) k_ads_persistent(const __grid_constant__ 
         o2.diff = A.step_diff;
         for (int u = (int)blockIdx.x; u < units; u += (int)gridDim.x)
         {
-            double rmax = 0.0;
+            float rmax = 0.0f;
             if (u < A.ntiles) rmax = o.parity ? ads_psi_tile<1>(A.L, A.C, o1, u) : ads_psi_tile<0>(A.L, A.C, o1, u);
             else
             {
