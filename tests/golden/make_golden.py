@@ -22,8 +22,12 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
   refstate_variants.npz  the reference's own runs with BGK / MRT collisions and
                     MDBB / BB walls, single block (64x64 test image) and
                     multi-block (block64 geometry)
+  refgrid_disks256_l3.npz  grid tables of the reference's own Grid2D / LB2D with
+                    the quadtree depth limit raised to 3 (oracle/_ref/ref_driver3)
+                    on a 256x256 seeded disk image (void x edges), with the image
+                    and its fields
 
-Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants]
+Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants|grid3]
 """
 import os
 import struct
@@ -178,6 +182,7 @@ def main():
     disk_state_fixture()
     disk_adsorption_fixture()
     variants_fixture(fx)
+    grid3_fixture()
     print("fixtures written to", HERE)
 
 
@@ -335,6 +340,31 @@ def properties_extra_fixture():
     np.savez_compressed(HERE / "refprops_extra.npz", dx=1e-9, mfp=5e-9, **out)
 
 
+def grid3_fixture():
+    """Three quadtree levels on a 256x256 disk image (radii 6-20, porosity 0.6,
+    seed 77, mean Kn 0.05, the two columns at either x edge void), built by the
+    reference's Grid2D with its depth limit raised to 3; grid only.  With solid
+    pixels on the x-periodic seam the reference's three-level build ends in a
+    segmentation fault (its interface tables then index outside its arrays)."""
+    sys.path.insert(0, str(ROOT))
+    from mantiis_gb300 import workloads
+
+    img = workloads.image(256, 6, 20, 0.6, 0.05, 77, open_x_edges=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "disks256"
+        write_col_major(f, img["pore"], img["kn"], img["locpore"])
+        # the fields as the reference read them (7 significant digits)
+        kn, lp = read_col_major(f / "Kn.dat", 256), read_col_major(f / "localporesize.dat", 256)
+        grid, _ = run_ref(f, 256, 0, True, dx=img["dx"], levels=3)
+    # the streaming link lists (330 k links) follow from conn and the boundary
+    # types and are left out to keep the file small; the wall and periodic lists stay
+    for k in ("stream_id", "stream_ic", "stream_loc"):
+        grid.pop(k)
+    grid["conn"] = grid["conn"].astype(np.int32)
+    np.savez_compressed(HERE / "refgrid_disks256_l3.npz", img_pore=img["pore"].astype(np.uint8), img_kn=kn,
+                        img_locpore=lp, dx=img["dx"], **grid)
+
+
 if __name__ == "__main__":
     if _ONLY:
         fx = dict(np.load(HERE / "fixture64.npz"))
@@ -342,6 +372,7 @@ if __name__ == "__main__":
          "properties_extra": lambda _: properties_extra_fixture(),
          "disk_state": lambda _: disk_state_fixture(),
          "disk_adsorption": lambda _: disk_adsorption_fixture(),
-         "variants": variants_fixture}[_ONLY](fx)
+         "variants": variants_fixture,
+         "grid3": lambda _: grid3_fixture()}[_ONLY](fx)
     else:
         main()

@@ -106,3 +106,23 @@ def test_three_level_grid_builds():
     assert (lv == 3).any() and (lv == 2).any() and (lv == 1).any()
     # every interface row points at existing cells
     assert (g.fine_rows[:, 1:] >= 0).all()
+
+
+def test_three_level_grid_matches_reference():
+    # the reference's own Grid2D / LB2D with the quadtree depth limit raised to 3
+    # (refgrid_disks256_l3.npz, a 256x256 disk image with void x edges): every
+    # table but the streaming link list, which the fixture leaves out
+    ref = load("refgrid_disks256_l3.npz")
+    p = default_params(multiblock=1, max_allowed_level=3, dx=float(ref["dx"]))
+    g = HostGrid(ref["img_pore"].astype(np.int32), ref["img_kn"], ref["img_locpore"], p)
+    assert g.max_level == 3
+    c = g.cells
+    assert g.n_cells == int(ref["n_cells"])
+    assert np.array_equal(np.stack([c["x"], c["y"]], 1), ref["ij"])
+    for k in ("level", "type", "is_buffer", "bnd", "lin", "conn", "kn"):
+        assert np.array_equal(c[k], ref[k]), k
+    for k in ("wall_id", "wall_ic", "per_id", "per_i2", "per_ic"):
+        assert np.array_equal(g.links[k], ref[k]), k
+    for k in ("coarse_rows", "fine_rows", "parent_child"):
+        assert np.array_equal(getattr(g, k), ref[k]), k
+    assert np.abs(c["tau"] - ref["tau"]).max() <= 1e-12

@@ -128,3 +128,22 @@ def test_reference_arm_loads_no_product_library():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["product_libraries_loaded"] == []
     assert "grid_oracle.cpp" in line["cpu_baseline"]["sample"]
+
+
+def test_grid_matches_reference_three_levels():
+    # the reference's own three-level Grid2D (depth limit raised to 3) on a
+    # 256x256 disk image with void x edges; the fixture holds every table but
+    # the streaming link list
+    ref = load("refgrid_disks256_l3.npz")
+    g = pygrid.GridTables(ref["img_pore"].astype(np.int32), ref["img_kn"], ref["img_locpore"], multiblock=True,
+                          max_allowed_level=3, dx=float(ref["dx"]))
+    c = g.cells
+    assert g.n_cells == int(ref["n_cells"]) and g.max_level == 3
+    assert np.array_equal(np.stack([c["x"], c["y"]], 1), ref["ij"])
+    for k in ("level", "type", "is_buffer", "bnd", "lin", "conn", "kn"):
+        assert np.array_equal(c[k], ref[k]), k
+    for k in ("wall_id", "wall_ic", "per_id", "per_i2", "per_ic"):
+        assert np.array_equal(g.links[k], ref[k]), k
+    for k in ("coarse_rows", "fine_rows", "parent_child"):
+        assert np.array_equal(getattr(g, k), ref[k]), k
+    assert np.abs(c["tau"] - ref["tau"]).max() <= 1e-12
