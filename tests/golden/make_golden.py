@@ -26,8 +26,11 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
                     the quadtree depth limit raised to 3 (oracle/_ref/ref_driver3)
                     on a 256x256 seeded disk image (void x edges), with the image
                     and its fields
+  refgrid_block128_l3.npz, refstate_block128_l3.npz  the same three-level build
+                    on a 128x128 block geometry, and the reference's own cell
+                    states after 1, 2 and 50 coarse steps
 
-Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants|grid3]
+Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants|grid3|state3]
 """
 import os
 import struct
@@ -183,6 +186,7 @@ def main():
     disk_adsorption_fixture()
     variants_fixture(fx)
     grid3_fixture()
+    state3_fixture()
     print("fixtures written to", HERE)
 
 
@@ -365,6 +369,31 @@ def grid3_fixture():
                         img_locpore=lp, dx=img["dx"], **grid)
 
 
+CASES3 = {
+    # name: (n, wall rows, obstacle rows/cols); three quadtree levels, grids on
+    # which the reference's interpolation stays inside its arrays
+    "block128_l3": (128, 2, (48, 80, 32, 64)),
+}
+
+
+def state3_fixture():
+    """The reference's own three-level run (oracle/_ref/ref_driver3, depth limit
+    raised to 3) on a block geometry: grid tables and cell states after 1, 2 and
+    50 coarse steps."""
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (n, wall, obst) in CASES3.items():
+            f = Path(tmp) / name
+            p, kn, lp = block_geometry(n, wall, obst)
+            write_col_major(f, p, kn, lp)
+            grid, states = run_ref(f, n, 50, True, levels=3, dump_steps=(1, 2, 50))
+            for k in ("stream_id", "stream_ic", "stream_loc"):
+                grid.pop(k)
+            grid["conn"] = grid["conn"].astype(np.int32)
+            np.savez_compressed(HERE / f"refgrid_{name}.npz", img_pore=p, img_kn=kn, img_locpore=lp, **grid)
+            np.savez_compressed(HERE / f"refstate_{name}.npz",
+                                **{f"{k}_{s}": v for s, st in states.items() for k, v in st.items()})
+
+
 if __name__ == "__main__":
     if _ONLY:
         fx = dict(np.load(HERE / "fixture64.npz"))
@@ -373,6 +402,7 @@ if __name__ == "__main__":
          "disk_state": lambda _: disk_state_fixture(),
          "disk_adsorption": lambda _: disk_adsorption_fixture(),
          "variants": variants_fixture,
-         "grid3": lambda _: grid3_fixture()}[_ONLY](fx)
+         "grid3": lambda _: grid3_fixture(),
+         "state3": lambda _: state3_fixture()}[_ONLY](fx)
     else:
         main()

@@ -88,6 +88,28 @@ def test_multiblock_matches_reference_code(case):
         assert e_ux < 5e-6 and e_rho < 1e-11 and e_f < 5e-12
 
 
+def test_three_levels_match_reference_code():
+    # the reference's own three-level run (depth limit raised to 3, oracle/_ref
+    # ref_driver3) on a 128x128 block geometry whose interpolation stays inside
+    # the reference's arrays (refstate_block128_l3.npz): 1, 2 and 50 coarse steps
+    ref = load("refgrid_block128_l3.npz")
+    st = load("refstate_block128_l3.npz")
+    s = Solver(ref["img_pore"], ref["img_kn"], ref["img_locpore"], default_params(multiblock=1, max_allowed_level=3))
+    assert s.info["max_level"] == 3
+    done = 0
+    for step in (1, 2, 50):
+        s.advance(step - done)
+        done = step
+        c = s.cells(with_f=True)
+        e_ux = rel_err(c["ux"], st[f"ux_{step}"])
+        e_rho = np.abs(c["rho"] - st[f"rho_{step}"]).max() / 0.2355
+        e_f = np.abs(c["f"] - st[f"f_{step}"]).max() / 0.2355
+        record(f"multiblock_block128_l3_{step}", ux=e_ux, rho=e_rho, f=e_f)
+        # measured (worst step): u_x 2.8e-7, rho 2.4e-10, f 2.2e-10 (FP32
+        # deviations: the coarse level's larger velocities)
+        assert e_ux < 3e-6 and e_rho < 2.5e-9 and e_f < 2.5e-9
+
+
 def oracle_pair(pore, steps, multiblock=0, levels=2, dx=1e-9, kn=None, lp=None, edge_fine=0):
     n = pore.shape[0]
     kn = np.where(pore == 1, 0.1, 0.0) if kn is None else kn

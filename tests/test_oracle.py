@@ -46,6 +46,30 @@ def test_oracle_multiblock_matches_reference_code(case):
     assert np.allclose(o.residuals(), st["residuals_50"], rtol=1e-9, atol=0)
 
 
+def test_oracle_three_levels_match_reference_code():
+    # the reference's own three-level run (depth limit raised to 3, oracle/_ref
+    # ref_driver3) on a 128x128 block geometry whose interpolation stays inside
+    # the reference's arrays: the oracle on its own grid tables, 50 coarse steps
+    from oracle.pygrid import GridTables
+
+    ref = load("refgrid_block128_l3.npz")
+    st = load("refstate_block128_l3.npz")
+    g = GridTables(ref["img_pore"], ref["img_kn"], ref["img_locpore"], multiblock=True, max_allowed_level=3)
+    assert g.max_level == 3 and g.n_cells == int(ref["n_cells"])
+    assert np.array_equal(g.cells["conn"], ref["conn"]) and np.array_equal(g.fine_rows, ref["fine_rows"])
+    o = for_grid(g, sim="transport", dx=1e-9)
+    done = 0
+    for step in (1, 2, 50):
+        o.run(step - done)
+        done = step
+        f = o.fields()
+        for name in ("rho", "ux", "uy"):
+            err = np.abs(f[name] - st[f"{name}_{step}"]).max()
+            assert err <= 1e-12, (step, name, err)
+        assert np.abs(f["f"] - st[f"f_{step}"]).max() <= 1e-12
+    assert np.allclose(o.residuals(), st["residuals_50"], rtol=1e-9, atol=0)
+
+
 def test_oracle_break_semantics(fixture64):
     # the loop stops right after the first step whose residual is below tol
     g = HostGrid(fixture64["pore"], fixture64["kn"], fixture64["locpore"], default_params(dx=1e-9))
