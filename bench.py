@@ -38,6 +38,7 @@ Multi-GPU (torchrun): every rank runs its own batch (weak scaling, no
 collective on the data path).
 """
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -423,6 +424,76 @@ def run_adsorption(args):
     }))
 
 
+def run_conv(args):
+    """The warm-start network's 3x3 convolutions at its layer sizes (8 images;
+    32..256 channels at 128^2..16^2 pixels, as the encoder-decoder's levels):
+    device time per call of the CUDA-core kernels and of the tcgen05 implicit
+    GEMMs, forward (bias + ReLU), data gradient and weight gradient, median of
+    `--steps` calls after `--warmup`; FLOP = 2 * 9 * cin * cout * pixels."""
+    import torch
+
+    from mantiis_gb300.surrogate import _ptr, cnn_lib
+
+    L = cnn_lib()
+    torch.manual_seed(0)
+    stream = torch.cuda.current_stream()
+    s = C.c_void_p(stream.cuda_stream)
+    layers = [(8, 32, 32, 128), (8, 64, 64, 64), (8, 128, 128, 32), (8, 256, 256, 16)]
+    out = []
+    for n, cin, cout, hw in layers:
+        x = torch.randn(n, cin, hw, hw, device="cuda")
+        dy = torch.randn(n, cout, hw, hw, device="cuda")
+        w = torch.randn(cout * cin * 9, device="cuda") * (2.0 / (9 * cin)) ** 0.5
+        w16 = torch.empty(w.numel(), dtype=torch.int16, device="cuda")
+        L.cnn_to_bf16(_ptr(w), _ptr(w16), w.numel(), s)
+        b = torch.zeros(cout, device="cuda")
+        y = torch.empty(n, cout, hw, hw, device="cuda")
+        dx = torch.empty_like(x)
+        dw = torch.zeros(cout * cin * 9, device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        calls = {
+            "forward_cuda_cores": lambda: L.cnn_conv3x3_forward(_ptr(x), _ptr(w16), _ptr(b), _ptr(y), n, cin, cout,
+                                                                hw, hw, 1, s),
+            "forward_tcgen05": lambda: L.cnn_conv3x3_forward_tc(_ptr(x), _ptr(w16), _ptr(b), _ptr(y), n, cin, cout,
+                                                                hw, hw, 1, s),
+            "data_grad_cuda_cores": lambda: L.cnn_conv3x3_backward_data(_ptr(dy), _ptr(w16), _ptr(dx), n, cin, cout,
+                                                                        hw, hw, s),
+            "data_grad_tcgen05": lambda: L.cnn_conv3x3_backward_data_tc(_ptr(dy), _ptr(w16), _ptr(dx), n, cin, cout,
+                                                                        hw, hw, s),
+            "weight_grad_cuda_cores": lambda: L.cnn_conv3x3_backward_weight(_ptr(x), _ptr(dy), _ptr(dw), _ptr(db), n,
+                                                                            cin, cout, hw, hw, s),
+            "weight_grad_tcgen05": lambda: L.cnn_conv3x3_backward_weight_tc(_ptr(x), _ptr(dy), _ptr(dw), _ptr(db),
+                                                                            n, cin, cout, hw, hw, s),
+        }
+        flop = 2.0 * 9 * cin * cout * n * hw * hw
+        row = {"images": n, "cin": cin, "cout": cout, "pixels": hw * hw, "gflop": flop / 1e9}
+        for name, fn in calls.items():
+            for _ in range(args.warmup):
+                if fn() != 0:
+                    raise RuntimeError(f"{name} failed")
+            times = []
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            ms = float(np.median(times))
+            row[name] = {"us": ms * 1e3, "tflops": flop / (ms / 1e3) / 1e12}
+        if L.cnn_tc_error() != 0:
+            raise RuntimeError("a tensor-core wait ran out")
+        out.append(row)
+    peak = None
+    try:
+        peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    print(json.dumps({"metric": "conv3x3_tflops", "unit": "TFLOP/s", "layers": out, "bf16_peak_tflops": peak,
+                      "note": "BF16 operands, FP32 accumulation; the tcgen05 path splits each FP32 activation "
+                              "into two BF16 parts (two MMAs per product)"}))
+
+
 def run_properties(args):
     from mantiis_gb300 import generate_disks, pore_properties, pore_properties_gpu
 
@@ -470,6 +541,8 @@ def main():
                     help="also run this many config4_steady images to steady state as one batch")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--properties", type=int, default=0, metavar="N")
+    ap.add_argument("--conv", action="store_true",
+                    help="time the warm-start network's convolutions (CUDA cores and tcgen05) instead")
     ap.add_argument("--adsorption", action="store_true", help="time the config-3 adsorption step instead")
     ap.add_argument("--ads-engine", type=int, default=1, choices=[0, 1],
                     help="adsorption engine: 1 one cooperative launch per call, 0 launches per pass")
@@ -486,6 +559,9 @@ def main():
         return
     if args.properties:
         run_properties(args)
+        return
+    if args.conv:
+        run_conv(args)
         return
     if args.adsorption:
         run_adsorption(args)
