@@ -252,15 +252,27 @@ def steady_batch_leg(count, stream, chunk=1000, tol=1e-6, max_steps=100000):
     from mantiis_gb300 import Batch, Solver, default_params, workloads
     from mantiis_gb300.surrogate import run_batch_to_steady
 
-    imgs = [workloads.config4_steady(i) for i in range(count)]
-    sol = []
-    for img in imgs:
+    from concurrent.futures import ThreadPoolExecutor
+
+    # the images and their contexts are made on all host cores (the generator,
+    # the pore properties and the grid construction are host code called
+    # through ctypes, which releases the interpreter); the plain-cell path is
+    # fixed to the 8x4 tiles, as timing the paths of contexts created at the
+    # same time would measure them against each other (all paths give
+    # bit-identical states)
+    def create(img):
         mb = img["levels"] > 1
         p = default_params(multiblock=int(mb), max_allowed_level=max(2, img["levels"]), dx=img["dx"],
-                           edge_fine=int(mb), concurrent=1)
-        s = Solver(img["pore"], img["kn"], img["locpore"], p)
+                           edge_fine=int(mb), concurrent=1, plain_path=2)
+        return Solver(img["pore"], img["kn"], img["locpore"], p)
+
+    t_setup = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        imgs = list(ex.map(workloads.config4_steady, range(count)))
+        sol = list(ex.map(create, imgs))
+    t_setup = time.perf_counter() - t_setup
+    for s in sol:
         s.set_stream(stream.cuda_stream)
-        sol.append(s)
     b = Batch(sol)
     b.set_stream(stream.cuda_stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -272,7 +284,7 @@ def steady_batch_leg(count, stream, chunk=1000, tol=1e-6, max_steps=100000):
     ms = e0.elapsed_time(e1)
     done = int(steps.max())
     lu = float(sum(s.info["lu_per_step"] for s in sol))
-    out = {"workload": STEADY_BATCH_WORKLOAD, "images": count,
+    out = {"workload": STEADY_BATCH_WORKLOAD, "images": count, "host_setup_seconds": t_setup,
            "criterion": f"relative permeability change below {tol:g} over {chunk} steps; a settled image "
                         f"leaves the batch",
            "settled": int((steps < max_steps).sum()), "coarse_steps": done, "gpu_seconds": ms / 1e3,
