@@ -292,7 +292,7 @@ def steady_batch_leg(count, stream, chunk=1000, tol=1e-6, max_steps=100000):
            "lu_if_all_stepped_to_the_end": lu * done, "lu_per_step": lu,
            "sides": [int(im["pore"].shape[0]) for im in imgs], "levels": [int(im["levels"]) for im in imgs],
            "steps_to_settle": [int(v) for v in steps], "permeability": [float(v) for v in k],
-           "positive": bool((np.asarray(k) > 0).all()), "finite": bool(np.isfinite(k).all())}
+           "positive": int((np.asarray(k) > 0).sum()), "finite": bool(np.isfinite(k).all())}
     b.close()
     for s in sol:
         s.close()

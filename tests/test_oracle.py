@@ -166,3 +166,30 @@ def test_oracle_variants_match_reference_code(fixture64, collision, wall, multib
     for name in ("ux", "uy"):
         scale = np.abs(st[f"{key}_{name}"]).max()
         assert np.abs(f[name] - st[f"{key}_{name}"]).max() <= 2e-9 * scale, name
+
+
+def test_reference_scheme_loses_mass_on_config4_image_186():
+    # 2 of the 256 config-4 steady images (186: 128^2, single block, porosity
+    # 0.35; 190: 128^2, two levels) settle to a negative permeability on the GPU;
+    # the FP64 restatement of the reference's step does the same on image 186: the
+    # mean flow runs against the force and the mass falls by ~1.4 % per 1000 steps,
+    # so under the reference's scheme the image has no physical steady state
+    import os
+
+    from mantiis_gb300 import workloads
+    from mantiis_gb300.surrogate import solver_params
+
+    d = workloads.config4_steady(186)
+    g = HostGrid(d["pore"], d["kn"], d["locpore"], solver_params(d))
+    o = for_grid(g, sim="transport", dx=d["dx"], threads=os.cpu_count() or 1)
+    keep = g.cells["is_buffer"] == 0
+
+    def mass_and_flow():
+        f = o.fields()
+        return f["rho"][keep].sum(), f["ux"][keep].mean()
+
+    o.run(1000)
+    m0, _ = mass_and_flow()
+    o.run(3000)
+    m1, ux = mass_and_flow()
+    assert ux < 0 and (m1 - m0) / m0 < -0.02
