@@ -249,27 +249,14 @@ def steady_batch_leg(count, stream, chunk=1000, tol=1e-6, max_steps=100000):
     CUDA events around the run."""
     import torch
 
-    from mantiis_gb300 import Batch, Solver, default_params, workloads
-    from mantiis_gb300.surrogate import run_batch_to_steady
+    from mantiis_gb300 import Batch, workloads
+    from mantiis_gb300.surrogate import make_solvers, run_batch_to_steady
 
-    from concurrent.futures import ThreadPoolExecutor
-
-    # the images and their contexts are made on all host cores (the generator,
-    # the pore properties and the grid construction are host code called
-    # through ctypes, which releases the interpreter); the plain-cell path is
-    # fixed to the 8x4 tiles, as timing the paths of contexts created at the
-    # same time would measure them against each other (all paths give
-    # bit-identical states)
-    def create(img):
-        mb = img["levels"] > 1
-        p = default_params(multiblock=int(mb), max_allowed_level=max(2, img["levels"]), dx=img["dx"],
-                           edge_fine=int(mb), concurrent=1, plain_path=2)
-        return Solver(img["pore"], img["kn"], img["locpore"], p)
-
+    # the images and their contexts are made on all host cores (8x4 plain-cell
+    # tiles fixed: surrogate.make_solvers)
     t_setup = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
-        imgs = list(ex.map(workloads.config4_steady, range(count)))
-        sol = list(ex.map(create, imgs))
+    imgs = workloads.generate(workloads.config4_steady, range(count))
+    sol = make_solvers(imgs, concurrent=1)
     t_setup = time.perf_counter() - t_setup
     for s in sol:
         s.set_stream(stream.cuda_stream)

@@ -21,6 +21,7 @@ ends), so the network learns asinh(target / scale) with a per-channel scale
 (UNet.scale, the median magnitude of the training targets).
 """
 import ctypes as C
+import os
 import time
 from pathlib import Path
 
@@ -533,13 +534,28 @@ def solver_params(d, **kw):
     return default_params(multiblock=int(mb), max_allowed_level=max(2, levels), dx=d["dx"], edge_fine=int(mb), **kw)
 
 
+def make_solvers(images, threads=None, **kw):
+    """Contexts of the images (workloads dicts), created on all host cores (the
+    grid construction is host code called through ctypes).  The plain-cell path
+    is fixed to the 8x4 tiles: timing the paths of contexts created at the same
+    time would measure them against each other, and every path gives
+    bit-identical states."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from .native import Solver
+
+    kw.setdefault("plain_path", 2)
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        return list(ex.map(lambda d: Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, **kw)), images))
+
+
 def steady_samples(images, chunk=1000, tol=1e-6, max_steps=100000, log=None):
     """Runs the images (workloads dicts) to steady state as one batch and
     returns (input, target, mask) of those that settled with a positive
     permeability (images of mixed sizes: a list, not an array)."""
-    from .native import Batch, Solver
+    from .native import Batch
 
-    sol = [Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, concurrent=1)) for d in images]
+    sol = make_solvers(images, concurrent=1)
     b = Batch(sol)
     t0 = time.perf_counter()
     steps, k = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
@@ -820,9 +836,9 @@ def coarse_density(solver, pore, block=COARSE):
 def coarse_samples(images, chunk=1000, tol=1e-6, max_steps=100000, log=None):
     """(coarse input, coarse density target, block mask) of the images that
     settle with a positive permeability, all stepped as one batch."""
-    from .native import Batch, Solver
+    from .native import Batch
 
-    sol = [Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, concurrent=1)) for d in images]
+    sol = make_solvers(images, concurrent=1)
     b = Batch(sol)
     t0 = time.perf_counter()
     steps, k = run_batch_to_steady(b, chunk=chunk, tol=tol, max_steps=max_steps)
@@ -924,7 +940,7 @@ def config5(train_images=64, eval_images=4, epochs=60, lr=1e-3, log=None):
     held-out 1024^2 two-level images workloads.config2_steady(0..eval-1)."""
     from . import workloads
 
-    samples = steady_samples([workloads.config4_steady(i) for i in range(train_images)], log=log)
+    samples = steady_samples(workloads.generate(workloads.config4_steady, range(train_images)), log=log)
     net = UNet(seed=5)
     ys = [y for _, y, _ in samples]
     ms = [m for _, _, m in samples]
@@ -962,8 +978,8 @@ def main(argv=None):
     if a.coarse:
         from . import workloads
 
-        samples = coarse_samples([workloads.config4_steady(i) for i in range(a.train)]
-                                 + [dict(workloads.config2_steady(i)) for i in range(8, 8 + a.train // 2)], log=log)
+        samples = coarse_samples(workloads.generate(workloads.config4_steady, range(a.train))
+                                 + workloads.generate(workloads.config2_steady, range(8, 8 + a.train // 2)), log=log)
         net, hist = train_coarse(samples, epochs=a.epochs, lr=a.lr, log=log)
         res = coarse_study(net, [workloads.config2_steady(i) for i in range(a.eval)], log=log)
         print(json.dumps(dict(train_images=len(samples), epochs=a.epochs, first_loss=hist[0], final_loss=hist[-1],

@@ -13,9 +13,21 @@ spacing dx is then chosen so that the mean Knudsen number over the void
 pixels equals the drawn one, and Kn = mfp / (H dx) per pixel
 (include/shape.hpp:245-246).
 """
+import os
+
 import numpy as np
 
 from .native import generate_disks, pore_properties, units
+
+
+def generate(make, indices, threads=None):
+    """make(i) for every index in order, on all host cores: the generator and
+    the pore properties are host code called through ctypes, which releases the
+    interpreter; the images are those of a plain loop."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        return list(ex.map(make, indices))
 
 
 def image(n, rmin, rmax, porosity, kn_mean, seed, open_x_edges=False):
