@@ -311,11 +311,15 @@ int mgpu_pore_properties_gpu(const int32_t *pore, int n, double dx, double mfp, 
 int mgpu_generate_disks(int n, double rmin, double rmax, double porosity, uint64_t seed, int32_t *pore_out);
 /* Same with flags: MGPU_DISKS_PERIODIC_X makes the disks wrap across the
  * x-periodic edge, so the image is itself x-periodic; MGPU_DISKS_OPEN_X_EDGES
- * keeps the two columns at either x edge void (solid pixels on the x-periodic
- * seam make the reference's wall-then-periodic order lose mass there, so such
- * images have no steady state). */
+ * keeps disks off the two columns at either x edge (solid pixels on the
+ * x-periodic seam make the reference's wall-then-periodic order lose mass
+ * there: a wall link's share lands in a population the periodic copy then
+ * overwrites, so such images have no steady state); MGPU_DISKS_WIDE_X_EDGES
+ * keeps them off three columns.  The fill of untabulated neighbourhoods can
+ * still put solid pixels on the seam: callers check the result. */
 #define MGPU_DISKS_PERIODIC_X 1
 #define MGPU_DISKS_OPEN_X_EDGES 2
+#define MGPU_DISKS_WIDE_X_EDGES 4
 int mgpu_generate_disks_ex(int n, double rmin, double rmax, double porosity, uint64_t seed, int flags,
                            int32_t *pore_out);
 

@@ -246,7 +246,8 @@ int mgpu_generate_disks_ex(int n, double rmin, double rmax, double porosity, uin
         if (!pore_out || n <= 0 || rmin <= 0 || rmax < rmin) throw std::invalid_argument("bad argument");
         std::vector<int> img =
             generate_disk_image(n, rmin, rmax, porosity, seed, (flags & MGPU_DISKS_PERIODIC_X) != 0,
-                                (flags & MGPU_DISKS_OPEN_X_EDGES) != 0);
+                                (flags & (MGPU_DISKS_OPEN_X_EDGES | MGPU_DISKS_WIDE_X_EDGES)) != 0,
+                                (flags & MGPU_DISKS_WIDE_X_EDGES) != 0 ? 3 : 2);
         std::copy(img.begin(), img.end(), pore_out);
         return MGPU_OK;
     });

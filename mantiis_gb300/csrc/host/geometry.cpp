@@ -312,7 +312,7 @@ int64_t fill_untabulated_pixels(std::vector<int> &img, int n)
 }
 
 std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed, bool periodic_x,
-                                     bool open_x_edges)
+                                     bool open_x_edges, int edge_margin)
 {
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<double> ur(rmin, rmax), uc(0.0, (double)n);
@@ -346,7 +346,7 @@ std::vector<int> generate_disk_image(int n, double rmin, double rmax, double por
             {
                 // x-periodic disks also cover the columns they reach across the edge
                 const int j = ((jj % n) + n) % n;
-                if (open_x_edges && (j < 2 || j >= n - 2)) continue;
+                if (open_x_edges && (j < edge_margin || j >= n - edge_margin)) continue;
                 double dy = i - cy, dxv = std::fabs(j - cx);
                 if (periodic_x) dxv = std::min(dxv, (double)n - dxv);
                 if (dy * dy + dxv * dxv <= r * r && img[(size_t)i * n + j])

@@ -61,10 +61,12 @@ std::vector<int> shrink_binary(const std::vector<int> &img, int n, int factor);
 // solid) until the porosity is at most `porosity`.  Void pixels whose
 // 9-neighbour wall pattern is not one of the 52 tabulated boundary types are
 // then filled (the reference rejects such images, include/grid.hpp:1146-1150).
-// periodic_x: disks wrap across the x-periodic edge; open_x_edges: the two
-// columns on either x edge stay void (no solid pixel on the periodic seam)
+// periodic_x: disks wrap across the x-periodic edge; open_x_edges: no disk
+// covers the `edge_margin` columns on either x edge (2 by default), which keeps
+// the periodic seam free of solid pixels unless the fill of untabulated
+// neighbourhoods puts some back there
 std::vector<int> generate_disk_image(int n, double rmin, double rmax, double porosity, uint64_t seed,
-                                     bool periodic_x = false, bool open_x_edges = false);
+                                     bool periodic_x = false, bool open_x_edges = false, int edge_margin = 2);
 
 // Fills void pixels whose neighbour pattern (periodic in x and y, as the
 // grid's neighbour table) is not tabulated, until none is left; returns the

@@ -196,11 +196,14 @@ def pore_properties_gpu(pore, dx, mfp, stream=None, return_iterations=False):
     return (lp, kn, it.value) if return_iterations else (lp, kn)
 
 
-def generate_disks(n, rmin, rmax, porosity, seed, periodic_x=False, open_x_edges=False):
+def generate_disks(n, rmin, rmax, porosity, seed, periodic_x=False, open_x_edges=False, edge_margin=2):
     """Seeded disk packing; periodic_x wraps the disks across the x-periodic
-    edge, open_x_edges keeps the two columns at either x edge void."""
+    edge, open_x_edges keeps disks off the `edge_margin` (2 or 3) columns at
+    either x edge."""
+    if edge_margin not in (2, 3):
+        raise ValueError("edge_margin must be 2 or 3")
     out = np.zeros(n * n, dtype=np.int32)
-    flags = (1 if periodic_x else 0) | (2 if open_x_edges else 0)
+    flags = (1 if periodic_x else 0) | ((4 if edge_margin == 3 else 2) if open_x_edges else 0)
     _host_check(lib().mgpu_generate_disks_ex(n, rmin, rmax, porosity, seed, flags, out))
     return out.reshape(n, n)
 
