@@ -73,12 +73,13 @@ def config4_steady(index=0):
     """A config-4 image on which the reference's scheme reaches a steady state:
     side in {128, ..., 2048}, disk radii n/256..n/32 (at least 2..4),
     porosity U[0.45, 0.75], the two columns at either x edge void, one or two
-    quadtree levels.  Kn is
-    kept where the reference's scheme settles: single block log-uniform in
-    [0.01, 0.12], two levels U[0.01, 0.02] x min(1024 / n, 2) (the relaxation
-    times of config2_steady).  At larger Kn the FP64 oracle itself finds no
-    steady state on such images: a 128^2 single-block image at Kn 1.48 loses
-    0.7 % of its mass per 1000 steps and its mean flow runs against the force."""
+    quadtree levels.  Kn is kept where the images were seen to settle within
+    100 k steps: single block log-uniform in [0.01, 0.12], two levels
+    U[0.01, 0.02] x min(1024 / n, 2) (the relaxation times of config2_steady;
+    larger two-level Kn diverges at the coarse/fine exchange).  A solid pixel
+    on the x-periodic seam makes the reference's order lose mass (a wall link's
+    share lands in a population the periodic copy overwrites): such an image
+    has no steady state, so the seam columns are kept void."""
     rng = np.random.default_rng(4500 + index)
     n = int(rng.choice([128, 256, 512, 1024, 2048]))
     phi = rng.uniform(0.45, 0.75)
