@@ -25,6 +25,8 @@ A bench step is one coarse time step of every image of the batch.
             GPU seconds, permeability
   steady_batch  (--steady-batch N) N config4_steady images as one batch to
             the same criterion
+  config3   the adsorption step of config 3 (512^2 Shan-Chen image), MLUPS
+            over --adsorption-steps steps (the --adsorption run's line)
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference's step)
             on the host cores, on a bounded sample of the same workload, with
             all threads and with one
@@ -369,12 +371,12 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def run_adsorption(args):
+def adsorption_leg(steps, warmup, engine):
     """Config 3 (Shan-Chen adsorption, 512x512 seeded disk image, porosity 0.6,
     psi = rho0 (1 - exp(-rho/rho0)), G = -4.5, G_ads = -0.5, rho = 0.5 +- 1e-3):
     MLUPS of the two-pass adsorption step with the per-step density residual,
-    device-timed over K steps, and the roofline of the step (80 B per update:
-    72 B of populations and the psi plane written and read)."""
+    device-timed over `steps` steps, and the roofline of the step (80 B per
+    update: 72 B of populations and the psi plane written and read)."""
     import torch
 
     from mantiis_gb300 import SIM_ADSORPTION, Solver, default_params
@@ -385,18 +387,17 @@ def run_adsorption(args):
     p = default_params(dx=img["dx"], simulation=SIM_ADSORPTION, rho_init=0.5, fbody=0.0, psi_form=1, rho_psi=0.5,
                        g_ff=-4.5 / 18, g_fs=3 * -0.5, check_every=1)
     stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     s = Solver(img["pore"], img["kn"], img["locpore"], p)
     s.set_stream(stream.cuda_stream)
-    s.set_engine(args.ads_engine)
+    s.set_engine(engine)
     rng = np.random.default_rng(3000)
     rho = 0.5 + rng.uniform(-1e-3, 1e-3, s.n_cells)
     s.set_equilibrium(rho, np.zeros_like(rho), np.zeros_like(rho))
-    s.advance(args.warmup)
+    s.advance(warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    s.advance(args.steps)
+    s.advance(steps)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
@@ -404,23 +405,27 @@ def run_adsorption(args):
     mass = float(s.observables()["mass"])
     s.close()
     peak, peak_kind = peaks()
-    achieved = 80.0 * cells * args.steps / (ms / 1e3) / 1e9
-    print(json.dumps({
-        "metric": "MLUPS", "value": cells * args.steps / (ms / 1e3) / 1e6, "unit": "MLUPS", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+    achieved = 80.0 * cells * steps / (ms / 1e3) / 1e9
+    return {
+        "metric": "MLUPS", "value": cells * steps / (ms / 1e3) / 1e6, "unit": "MLUPS", "n_gpus": 1,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "config3: 512x512 seeded disk image, porosity 0.6, Shan-Chen adsorption, "
                                "exponential psi (rho0 0.5), G -4.5, G_ads -0.5, rho 0.5 +- 1e-3",
                    "cells": cells, "l2": "state L2-resident (one 512^2 image)",
-                   "engine": "one cooperative launch per call (grid barriers between passes)" if args.ads_engine
+                   "engine": "one cooperative launch per call (grid barriers between passes)" if engine
                    else "launches per pass, pairs of steps from a CUDA graph"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "kernel": "adsorption step (" + ("k_ads_persistent" if args.ads_engine else
+                     "kernel": "adsorption step (" + ("k_ads_persistent" if engine else
                                                       "k_ads_psi + k_ads_step") + ")",
                      "bytes_per_unit": 80.0},
         "mass_after": mass,
-    }))
+    }
+
+
+def run_adsorption(args):
+    print(json.dumps(adsorption_leg(args.steps, args.warmup, args.ads_engine)))
 
 
 def run_conv(args):
@@ -543,6 +548,8 @@ def main():
     ap.add_argument("--conv", action="store_true",
                     help="time the warm-start network's convolutions (CUDA cores and tcgen05) instead")
     ap.add_argument("--adsorption", action="store_true", help="time the config-3 adsorption step instead")
+    ap.add_argument("--adsorption-steps", type=int, default=2000,
+                    help="steps of the config-3 adsorption leg of the headline run (0 = skip it)")
     ap.add_argument("--ads-engine", type=int, default=1, choices=[0, 1],
                     help="adsorption engine: 1 one cooperative launch per call, 0 launches per pass")
     # plain-cell kernels: -1 times all three at creation (autotune); a fixed
@@ -723,6 +730,11 @@ def main():
     if rank == 0 and args.steady_batch > 0:
         steady_batch = steady_batch_leg(args.steady_batch, stream)
 
+    # config 3 beside the headline: the adsorption step of one 512^2 image
+    config3 = None
+    if rank == 0 and args.adsorption_steps > 0:
+        config3 = adsorption_leg(args.adsorption_steps, 10, args.ads_engine)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -763,6 +775,8 @@ def main():
                        "seconds_timed": total_ms / 1e3},
             "steady_state": steady,
             **({"steady_batch": steady_batch} if steady_batch else {}),
+            **({"config3": {k: config3[k] for k in ("value", "unit", "ms_per_step", "steps", "roofline", "config",
+                                                    "mass_after")}} if config3 else {}),
             "cpu_baseline": cpu,
             "e2e": e2e_obj,
             "clocks": clocks,
