@@ -32,9 +32,10 @@ _cnn = None
 # True: the convolutions' forward and data gradient run as the tcgen05 implicit
 # GEMMs (cnn_conv3x3_*_tc).  Their operand staging (the threads gather the patch
 # matrix and split it into two BF16 parts in shared memory, one stage) bounds
-# them at 7-12 TFLOP/s, below the CUDA-core kernels' 13-15 at this network's
-# layer sizes (8 x 32..256 channels, 16^2..128^2 pixels), so those stay the
-# default; both agree with FP64 to within 6e-6 of the largest output.
+# them at 6-12 TFLOP/s, below the CUDA-core kernels' 10-14.5 at this network's
+# layer sizes (8 x 32..256 channels, 16^2..128^2 pixels; bench.py --conv), so
+# those stay the default; both agree with FP64 to within 6e-6 of the largest
+# output.
 TENSOR_CORES = False
 
 _P = C.c_void_p
