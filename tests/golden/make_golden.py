@@ -26,11 +26,12 @@ the reference at REF_DIR and oracle/_ref built: `make -C oracle`).
                     the quadtree depth limit raised to 3 (oracle/_ref/ref_driver3)
                     on a 256x256 seeded disk image (void x edges), with the image
                     and its fields
+  refgrid_disks256_l2.npz  the unpatched reference's two-level grid of that image
   refgrid_block128_l3.npz, refstate_block128_l3.npz  the same three-level build
                     on a 128x128 block geometry, and the reference's own cell
                     states after 1, 2 and 50 coarse steps
 
-Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants|grid3|state3]
+Usage: python tests/golden/make_golden.py REF_DIR [--only properties|properties_extra|disk_state|disk_adsorption|coupled|variants|grid3|grid2_disks|state3]
 """
 import os
 import struct
@@ -186,6 +187,7 @@ def main():
     disk_adsorption_fixture()
     variants_fixture(fx)
     grid3_fixture()
+    grid2_disks_fixture()
     state3_fixture()
     print("fixtures written to", HERE)
 
@@ -344,6 +346,25 @@ def properties_extra_fixture():
     np.savez_compressed(HERE / "refprops_extra.npz", dx=1e-9, mfp=5e-9, **out)
 
 
+def grid2_disks_fixture():
+    """Two quadtree levels (the reference's own depth limit, unpatched
+    ref_driver) on the 256x256 disk image of grid3_fixture; grid only."""
+    sys.path.insert(0, str(ROOT))
+    from mantiis_gb300 import workloads
+
+    img = workloads.image(256, 6, 20, 0.6, 0.05, 77, open_x_edges=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        f = Path(tmp) / "disks256"
+        write_col_major(f, img["pore"], img["kn"], img["locpore"])
+        kn, lp = read_col_major(f / "Kn.dat", 256), read_col_major(f / "localporesize.dat", 256)
+        grid, _ = run_ref(f, 256, 0, True, dx=img["dx"], levels=2)
+    for k in ("stream_id", "stream_ic", "stream_loc"):
+        grid.pop(k)
+    grid["conn"] = grid["conn"].astype(np.int32)
+    np.savez_compressed(HERE / "refgrid_disks256_l2.npz", img_pore=img["pore"].astype(np.uint8), img_kn=kn,
+                        img_locpore=lp, dx=img["dx"], **grid)
+
+
 def grid3_fixture():
     """Three quadtree levels on a 256x256 disk image (radii 6-20, porosity 0.6,
     seed 77, mean Kn 0.05, the two columns at either x edge void), built by the
@@ -403,6 +424,7 @@ if __name__ == "__main__":
          "disk_adsorption": lambda _: disk_adsorption_fixture(),
          "variants": variants_fixture,
          "grid3": lambda _: grid3_fixture(),
+         "grid2_disks": lambda _: grid2_disks_fixture(),
          "state3": lambda _: state3_fixture()}[_ONLY](fx)
     else:
         main()

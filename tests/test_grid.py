@@ -108,14 +108,16 @@ def test_three_level_grid_builds():
     assert (g.fine_rows[:, 1:] >= 0).all()
 
 
-def test_three_level_grid_matches_reference():
-    # the reference's own Grid2D / LB2D with the quadtree depth limit raised to 3
-    # (refgrid_disks256_l3.npz, a 256x256 disk image with void x edges): every
-    # table but the streaming link list, which the fixture leaves out
-    ref = load("refgrid_disks256_l3.npz")
-    p = default_params(multiblock=1, max_allowed_level=3, dx=float(ref["dx"]))
+@pytest.mark.parametrize("levels", [2, 3])
+def test_disk_image_grid_matches_reference(levels):
+    # the reference's own Grid2D / LB2D on a 256x256 disk image with void x
+    # edges: two levels from the unmodified reference, three with its quadtree
+    # depth limit raised to 3 (refgrid_disks256_l<levels>.npz); every table but
+    # the streaming link list, which the fixtures leave out
+    ref = load(f"refgrid_disks256_l{levels}.npz")
+    p = default_params(multiblock=1, max_allowed_level=levels, dx=float(ref["dx"]))
     g = HostGrid(ref["img_pore"].astype(np.int32), ref["img_kn"], ref["img_locpore"], p)
-    assert g.max_level == 3
+    assert g.max_level == levels
     c = g.cells
     assert g.n_cells == int(ref["n_cells"])
     assert np.array_equal(np.stack([c["x"], c["y"]], 1), ref["ij"])

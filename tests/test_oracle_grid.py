@@ -130,15 +130,16 @@ def test_reference_arm_loads_no_product_library():
     assert "grid_oracle.cpp" in line["cpu_baseline"]["sample"]
 
 
-def test_grid_matches_reference_three_levels():
-    # the reference's own three-level Grid2D (depth limit raised to 3) on a
-    # 256x256 disk image with void x edges; the fixture holds every table but
-    # the streaming link list
-    ref = load("refgrid_disks256_l3.npz")
+@pytest.mark.parametrize("levels", [2, 3])
+def test_grid_matches_reference_disk_image(levels):
+    # the reference's own Grid2D on a 256x256 disk image with void x edges: two
+    # levels from the unmodified reference, three with its depth limit raised to
+    # 3; the fixtures hold every table but the streaming link list
+    ref = load(f"refgrid_disks256_l{levels}.npz")
     g = pygrid.GridTables(ref["img_pore"].astype(np.int32), ref["img_kn"], ref["img_locpore"], multiblock=True,
-                          max_allowed_level=3, dx=float(ref["dx"]))
+                          max_allowed_level=levels, dx=float(ref["dx"]))
     c = g.cells
-    assert g.n_cells == int(ref["n_cells"]) and g.max_level == 3
+    assert g.n_cells == int(ref["n_cells"]) and g.max_level == levels
     assert np.array_equal(np.stack([c["x"], c["y"]], 1), ref["ij"])
     for k in ("level", "type", "is_buffer", "bnd", "lin", "conn", "kn"):
         assert np.array_equal(c[k], ref[k]), k
