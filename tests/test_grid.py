@@ -128,3 +128,20 @@ def test_disk_image_grid_matches_reference(levels):
     for k in ("coarse_rows", "fine_rows", "parent_child"):
         assert np.array_equal(getattr(g, k), ref[k]), k
     assert np.abs(c["tau"] - ref["tau"]).max() <= 1e-12
+
+
+def test_three_level_block_grid_matches_reference():
+    # the three-level block geometry of refstate_block128_l3.npz (the reference's
+    # own run with its depth limit raised to 3)
+    ref = load("refgrid_block128_l3.npz")
+    g = HostGrid(ref["img_pore"], ref["img_kn"], ref["img_locpore"], default_params(multiblock=1, max_allowed_level=3))
+    assert g.max_level == 3 and g.n_cells == int(ref["n_cells"])
+    c = g.cells
+    for k in ("level", "type", "is_buffer", "bnd", "lin", "conn"):
+        assert np.array_equal(c[k], ref[k]), k
+    for k in ("wall_id", "wall_ic", "per_id", "per_i2", "per_ic"):
+        assert np.array_equal(g.links[k], ref[k]), k
+    for k in ("coarse_rows", "fine_rows", "parent_child"):
+        assert np.array_equal(getattr(g, k), ref[k]), k
+    assert np.abs(c["tau"] - ref["tau"]).max() <= 1e-12
+    assert sum(g.diagnostics.values()) == 0
