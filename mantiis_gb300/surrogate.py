@@ -543,11 +543,19 @@ def make_solvers(images, threads=None, **kw):
     bit-identical states."""
     from concurrent.futures import ThreadPoolExecutor
 
+    import torch
+
     from .native import Solver
 
     kw.setdefault("plain_path", 2)
+    device = torch.cuda.current_device()  # a context lives on its creating thread's current device
+
+    def create(d):
+        torch.cuda.set_device(device)
+        return Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, **kw))
+
     with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
-        return list(ex.map(lambda d: Solver(d["pore"], d["kn"], d["locpore"], solver_params(d, **kw)), images))
+        return list(ex.map(create, images))
 
 
 def steady_samples(images, chunk=1000, tol=1e-6, max_steps=100000, log=None):
