@@ -148,3 +148,35 @@ def test_grid_matches_reference_disk_image(levels):
     for k in ("coarse_rows", "fine_rows", "parent_child"):
         assert np.array_equal(getattr(g, k), ref[k]), k
     assert np.abs(c["tau"] - ref["tau"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_grid_and_properties_agree_on_random_images(seed):
+    # two independent restatements of the reference's grid construction (the
+    # product's host builder and the oracle's) on seeded random disk images:
+    # sizes 32..128, porosity 0.45..0.8, void x edges or not, one to three
+    # levels, with and without edge_fine; where one rejects an image (an
+    # untabulated boundary pattern), so must the other
+    from mantiis_gb300 import HostGrid, MantiisError, default_params, generate_disks, pore_properties
+
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.choice([32, 64, 128]))
+    pore = generate_disks(n, 2.0, max(3.0, n / 16), float(rng.uniform(0.45, 0.8)), 7000 + seed,
+                          open_x_edges=bool(seed % 2))
+    lp_a, kn_a = pore_properties(pore, 1e-9, 5e-9)
+    lp_b, kn_b = pygrid.pore_properties(pore, 1e-9, 5e-9)
+    assert np.array_equal(lp_a, lp_b) and np.array_equal(kn_a, kn_b)
+    levels = int(rng.integers(1, 4))
+    edge_fine = bool(rng.integers(0, 2)) and levels > 1
+    kn = np.where(pore == 1, kn_a, 0.0)
+    p = default_params(multiblock=int(levels > 1), max_allowed_level=max(levels, 2), dx=1e-9, edge_fine=int(edge_fine))
+    try:
+        want = HostGrid(pore, kn, lp_a, p)
+    except MantiisError as e:
+        with pytest.raises(RuntimeError, match=str(e).split(":")[-1].strip()[:20]):
+            pygrid.GridTables(pore, kn, lp_a, multiblock=levels > 1, max_allowed_level=max(levels, 2),
+                              edge_fine=edge_fine)
+        return
+    got = pygrid.GridTables(pore, kn, lp_a, multiblock=levels > 1, max_allowed_level=max(levels, 2),
+                            edge_fine=edge_fine)
+    assert same_tables(got, want) == []
