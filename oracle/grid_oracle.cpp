@@ -22,7 +22,7 @@
 #include <omp.h>
 
 // the reference's boundary-type tables (include/system_files/*.txt), compiled in
-#include "../mantiis_gb300/csrc/boundary_tables.h"
+#include "reference_tables.h"
 
 namespace
 {
@@ -666,8 +666,8 @@ void GridBuilder::build()
         for (int k = 0; k < 9; k++) code = code * 2 + (T.conn[(size_t)c * 9 + order[k]] == -1 ? 0 : 1);
         if (code == 511) continue;
         int t = 0;
-        while (t < MANTIIS_N_BND_TYPES && MANTIIS_BND_CODES[t] != code) t++;
-        if (t == MANTIIS_N_BND_TYPES) throw std::runtime_error("[ERROR]: Boundary type is not contained.");
+        while (t < ORACLE_N_BND_TYPES && ORACLE_BND_CODES[t] != code) t++;
+        if (t == ORACLE_N_BND_TYPES) throw std::runtime_error("[ERROR]: Boundary type is not contained.");
         T.bnd[c] = t;
     }
 
@@ -682,7 +682,7 @@ void GridBuilder::build()
             const i64 nb = T.conn[(size_t)i * 9 + q];
             // a buffer cell has no boundary type; its wall links read ifStream[-1]
             // in the reference and are taken as walls here
-            const bool streams = b == -1 ? (nb != -1) : MANTIIS_IFSTREAM[b][q] != 0;
+            const bool streams = b == -1 ? (nb != -1) : ORACLE_IFSTREAM[b][q] != 0;
             if (nb >= 0 && nb < N)
             {
                 const bool xp = std::abs(T.x[i] - T.x[nb]) > thr, yp = std::abs(T.y[i] - T.y[nb]) > thr;

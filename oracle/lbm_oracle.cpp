@@ -13,7 +13,7 @@
 
 #include "shim/interpolation.h" // the ALGLIB bicubic spline restatement
 // the boundary-type tables (identical numbers to include/system_files/*.txt)
-#include "../mantiis_gb300/csrc/boundary_tables.h"
+#include "reference_tables.h"
 
 namespace
 {
@@ -643,13 +643,13 @@ void *oracle_create(const OracleGrid *g, const OracleParams *p, const double *rh
         }
         for (auto &e : b[i]) o->bfIC[i].push_back(e.first);
     }
-    o->icsr.assign(MANTIIS_N_BND_TYPES, std::vector<int>(9));
-    o->xy_norm.assign(MANTIIS_N_BND_TYPES, std::vector<double>(2));
-    for (int t = 0; t < MANTIIS_N_BND_TYPES; t++)
+    o->icsr.assign(ORACLE_N_BND_TYPES, std::vector<int>(9));
+    o->xy_norm.assign(ORACLE_N_BND_TYPES, std::vector<double>(2));
+    for (int t = 0; t < ORACLE_N_BND_TYPES; t++)
     {
-        for (int q = 0; q < 9; q++) o->icsr[t][q] = MANTIIS_ICSR[t][q];
-        o->xy_norm[t][0] = MANTIIS_XY_NORM[t][0];
-        o->xy_norm[t][1] = MANTIIS_XY_NORM[t][1];
+        for (int q = 0; q < 9; q++) o->icsr[t][q] = ORACLE_ICSR[t][q];
+        o->xy_norm[t][0] = ORACLE_XY_NORM[t][0];
+        o->xy_norm[t][1] = ORACLE_XY_NORM[t][1];
     }
     o->initialize(rho_init);
     return o;
