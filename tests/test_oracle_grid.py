@@ -180,3 +180,22 @@ def test_grid_and_properties_agree_on_random_images(seed):
     got = pygrid.GridTables(pore, kn, lp_a, multiblock=levels > 1, max_allowed_level=max(levels, 2),
                             edge_fine=edge_fine)
     assert same_tables(got, want) == []
+
+
+def test_oracle_tables_hold_the_products_numbers():
+    # the oracle's copy of the reference's boundary-type tables and the product's
+    # (both written from include/system_files) hold the same numbers
+    import re
+
+    def arrays(path, prefix):
+        txt = path.read_text()
+        out = {}
+        for name in ("BND_CODES", "IFSTREAM", "ICSR", "XY_NORM"):
+            blk = txt[txt.index(prefix + name):]
+            blk = blk[blk.index("=") + 1:blk.index("};")]
+            out[name] = [float(v) for v in re.findall(r"-?\d+(?:\.\d+)?(?:[eE]-?\d+)?", blk)]
+        return out
+
+    a = arrays(ROOT / "oracle" / "reference_tables.h", "ORACLE_")
+    b = arrays(ROOT / "mantiis_gb300" / "csrc" / "boundary_tables.h", "MANTIIS_")
+    assert a == b and len(a["BND_CODES"]) == 52 and len(a["IFSTREAM"]) == 52 * 9
